@@ -1,0 +1,234 @@
+/*
+ * infoli_gpu.h -- C ABI of the GB300 InfOli network-update library
+ * (libinfoli_gpu.so).
+ *
+ * The reference simulator has no library API: its per-step network update is
+ * inline in main() of src/openmp/infoli.c.  Each entry point below replaces one
+ * piece of that program, cited as file:line inside the reference project.
+ * Plain C types only (pointers, sizes); no CUDA or framework types appear.
+ *
+ * Conventions
+ *   - Every call returns an int status: INFOLI_OK (0) or a negative
+ *     INFOLI_ERR_* code; infoli_last_error() gives a message for the calling
+ *     thread.  Nothing here calls exit() (the reference printf()s and exits).
+ *   - Host arrays passed in are copied; the caller keeps ownership.
+ *   - Device memory is owned by the library and released by *_destroy.
+ *   - A handle is not thread-safe; distinct handles may be used from distinct
+ *     threads (each has its own CUDA streams).
+ *   - Per-cell state is exchanged as 19 SoA arrays of n floats each, in the
+ *     order of bin/default.conf lines 24-42 (INFOLI_S_* below).
+ */
+#ifndef INFOLI_GPU_H
+#define INFOLI_GPU_H
+
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define INFOLI_ABI_VERSION 1
+
+/* status codes */
+#define INFOLI_OK 0
+#define INFOLI_ERR_ARG (-1)       /* invalid argument */
+#define INFOLI_ERR_CUDA (-2)      /* CUDA runtime error / no usable GPU */
+#define INFOLI_ERR_NOMEM (-3)     /* host or device allocation failed */
+#define INFOLI_ERR_TIMEOUT (-4)   /* a device-side wait gave up (error recorded, kernel returned) */
+#define INFOLI_ERR_FILE (-5)      /* a file could not be opened / read */
+#define INFOLI_ERR_CONFIG (-6)    /* malformed configuration / input file */
+#define INFOLI_ERR_CAPACITY (-7)  /* request exceeds a configured capacity (HBM budget, slots) */
+#define INFOLI_ERR_STATE (-8)     /* call not valid in the handle's current state */
+
+/* number of model constants / per-cell state arrays (bin/default.conf:1-23 / 24-42) */
+#define INFOLI_NPARAM 23
+#define INFOLI_NSTATE 19
+#define INFOLI_NCONF 42
+
+/* model constant indices (bin/default.conf:1-23; src/openmp/infoli.c:240-262) */
+enum {
+  INFOLI_P_DELTA = 0, INFOLI_P_CONDUCTANCE, INFOLI_P_C_M, INFOLI_P_G_NA_S, INFOLI_P_G_KDR_S,
+  INFOLI_P_G_K_S, INFOLI_P_G_LS, INFOLI_P_G_K_CA, INFOLI_P_G_CAH, INFOLI_P_G_LD, INFOLI_P_G_H,
+  INFOLI_P_G_NA_A, INFOLI_P_G_NA_R, INFOLI_P_G_K_A, INFOLI_P_G_LA, INFOLI_P_P1, INFOLI_P_P2,
+  INFOLI_P_G_INT, INFOLI_P_V_NA, INFOLI_P_V_K, INFOLI_P_V_CA, INFOLI_P_V_H, INFOLI_P_V_L
+};
+
+/* state array indices (bin/default.conf:24-42; src/openmp/infoli.c:267-292) */
+enum {
+  INFOLI_S_V_DEND = 0, INFOLI_S_CALCIUM_R, INFOLI_S_POTASSIUM_S, INFOLI_S_HCURRENT_Q,
+  INFOLI_S_CA2PLUS, INFOLI_S_I_CAH, INFOLI_S_G_CAL, INFOLI_S_V_SOMA, INFOLI_S_SODIUM_M,
+  INFOLI_S_SODIUM_H, INFOLI_S_POTASSIUM_N, INFOLI_S_POTASSIUM_P, INFOLI_S_POTASSIUM_X_S,
+  INFOLI_S_CALCIUM_K, INFOLI_S_CALCIUM_L, INFOLI_S_V_AXON, INFOLI_S_SODIUM_M_A,
+  INFOLI_S_SODIUM_H_A, INFOLI_S_POTASSIUM_X_A
+};
+
+/* trace selection bits for infoli_sim_run */
+#define INFOLI_TRACE_AXON 1 /* V_axon: what the reference prints (src/openmp/infoli.c:687) */
+#define INFOLI_TRACE_SOMA 2
+#define INFOLI_TRACE_DEND 4
+
+/* flags for infoli_sim_desc.flags */
+#define INFOLI_F_KAHAN 1     /* Kahan-compensated FP32 coupling sums */
+
+/* ------------------------------------------------------------------------ */
+/* library                                                                   */
+/* ------------------------------------------------------------------------ */
+
+/* Message describing the last failed call on this thread ("" if none). */
+const char* infoli_last_error(void);
+
+/* ABI version (INFOLI_ABI_VERSION) and a build description string. */
+int infoli_version(void);
+const char* infoli_build_info(void);
+
+/* Number of usable CUDA devices, or a negative status. */
+int infoli_device_count(void);
+
+/* ------------------------------------------------------------------------ */
+/* configuration and topology (host side)                                   */
+/* ------------------------------------------------------------------------ */
+
+/* Replaces read_parameters (src/utils/utils.c:137-160): reads the 42
+ * positional "NAME = value" lines of a default.conf-style file into
+ * values[42].  Names are not checked, as in the reference. */
+int infoli_read_parameters(const char* path, float values[INFOLI_NCONF]);
+
+/* Replaces read_g_CaL_from_file (src/utils/utils.c:124-135): reads up to n
+ * whitespace-separated floats into g_cal; cells beyond the end of the file
+ * keep their value (the reference leaves them at the default.conf value).
+ * Returns the number of values read (>= 0) or a negative status. */
+int infoli_read_gcal(const char* path, int n, float* g_cal);
+
+/* Replaces the built-in topology generator (src/openmp/infoli.c:337-375):
+ * srand(seed), then one rand() draw per ordered pair (receiver-major, sender
+ * ascending, self skipped); an edge exists when
+ * (float)rand()/(float)RAND_MAX <= p.  Output in CSR form: row_ptr[n+1] and
+ * col[] (capacity cap) with ascending senders per receiver.  *n_edges gets
+ * the edge count; if it exceeds cap, INFOLI_ERR_CAPACITY is returned and
+ * row_ptr is still complete.  Uses the C library's rand() exactly like the
+ * reference, so results are bit-identical for the same seed. */
+int infoli_gen_uniform(int n, float p, unsigned seed, int64_t* row_ptr, int32_t* col, int64_t cap,
+                       int64_t* n_edges);
+
+/* Synthetic 2-D grid topology (no counterpart in the reference's CLI; its
+ * nearest relatives are src/utils/utils.c:202-303 and
+ * tools/connectivity/2d_gaussian/conn_generator.c:43-128): rows x cols cells,
+ * id = row * cols + col; every other cell within `radius` is a sender with
+ * probability exp(-d^2 / (2 sigma^2)), one splitmix64 draw per candidate in
+ * ascending id.  Same output contract as infoli_gen_uniform. */
+int infoli_gen_grid_gaussian(int rows, int cols, float sigma, float radius, uint64_t seed, int64_t* row_ptr,
+                             int32_t* col, int64_t cap, int64_t* n_edges);
+
+/* Synthetic sparse topology: each receiver gets k distinct uniformly drawn
+ * senders (ascending ids); g (optional) gets per-edge conductances uniform in
+ * [g_lo, g_hi).  cap must be >= n * k. */
+int infoli_gen_fixed_degree(int n, int k, float g_lo, float g_hi, uint64_t seed, int64_t* row_ptr, int32_t* col,
+                            float* g, int64_t cap);
+
+/* Converts a dense receiver bitmask (row r = receiver, bit s of word s/32 =
+ * sender s, ceil(n/32) words per row) to CSR.  Same output contract as
+ * infoli_gen_uniform. */
+int infoli_bitmask_to_csr(int n, const uint32_t* bits, int64_t* row_ptr, int32_t* col, int64_t cap,
+                          int64_t* n_edges);
+
+/* ------------------------------------------------------------------------ */
+/* one simulation on the GPU                                                */
+/* ------------------------------------------------------------------------ */
+
+typedef struct infoli_sim infoli_sim;
+
+typedef struct {
+  int n_cells;
+  const float* params;       /* [INFOLI_NPARAM] model constants */
+  const float* init_state;   /* [INFOLI_NSTATE * n_cells] SoA, or NULL: broadcast init_values */
+  const float* init_values;  /* [INFOLI_NSTATE] used when init_state is NULL (conf lines 24-42) */
+  /* topology, CSR by receiver (the reference's cellCompParams,
+   * src/openmp/infoli.h:79-83: total_amount_of_neighbours / neighId /
+   * neighConductances) */
+  const int64_t* row_ptr;    /* [n_cells + 1] */
+  const int32_t* col;        /* [row_ptr[n]] sender ids */
+  const float* g;            /* [row_ptr[n]] per-edge conductance, or NULL */
+  float g_uniform;           /* conductance of every edge when g is NULL (CONDUCTANCE) */
+  int flags;                 /* INFOLI_F_* */
+  int device;                /* CUDA device ordinal */
+} infoli_sim_desc;
+
+/* Trace callback: called once per recorded step with the values of that step
+ * (n_cells floats per selected quantity, in the order axon, soma, dend of the
+ * selected bits).  step = the reference's simStep (0-based). */
+typedef void (*infoli_trace_cb)(void* user, int step, int what, const float* values, int n_cells);
+
+/* Replaces the setup half of main() (state arrays src/openmp/infoli.c:204-292,
+ * connectivity :306-375): uploads parameters, state and topology and plans
+ * the persistent step kernel. */
+int infoli_sim_create(const infoli_sim_desc* desc, infoli_sim** out);
+
+/* Stimulus.  Default: the reference's hard-coded pulse
+ * (src/openmp/infoli.c:482-485): 6 uA/cm2 for 20000 <= step < 20499. */
+int infoli_sim_set_stimulus_pulse(infoli_sim* s, int start_step, int end_step, float amp);
+/* Per-cell pulses: amp[c] for onset[c] <= step < onset[c] + duration. */
+int infoli_sim_set_stimulus_cells(infoli_sim* s, const float* amp, const int* onset, int duration);
+
+/* Replaces the time-step loop (src/openmp/infoli.c:478-698): advances
+ * n_steps explicit-Euler steps.  When trace_every > 0, the selected
+ * quantities are recorded after every step whose index is a multiple of
+ * trace_every (the reference's print rule, :682) and delivered to cb, in step
+ * order, from the calling thread; device->host trace copies run on a side
+ * stream while the next steps compute. */
+int infoli_sim_run(infoli_sim* s, int n_steps, int trace_every, int trace_what, infoli_trace_cb cb,
+                   void* user);
+
+/* Same as infoli_sim_run, writing the trace rows into a caller buffer
+ * out[rows][nq][n_cells] (nq = number of selected quantities); *rows_out
+ * gets the row count.  out may be NULL when trace_every <= 0. */
+int infoli_sim_run_into(infoli_sim* s, int n_steps, int trace_every, int trace_what, float* out,
+                        int64_t out_capacity_floats, int* rows_out);
+
+/* Copies the current state out / in ([INFOLI_NSTATE * n_cells] SoA). */
+int infoli_sim_get_state(infoli_sim* s, float* state_out);
+int infoli_sim_set_state(infoli_sim* s, const float* state_in);
+
+/* Next step index (the reference's simStep). */
+int infoli_sim_step(infoli_sim* s, int* step_out);
+
+/* Kernel timing of the last infoli_sim_run (CUDA events on the launch
+ * stream): total device milliseconds and number of kernel launches. */
+int infoli_sim_last_run_stats(infoli_sim* s, float* device_ms, int* launches);
+
+/* Plan summary: grid (CTAs), threads per CTA, total tiles, total chunks,
+ * dynamic shared memory bytes. */
+int infoli_sim_plan_info(infoli_sim* s, int* grid, int* threads, int* tiles, int* chunks,
+                         int64_t* smem_bytes);
+
+/* Device-side phase timers, the counterpart of the reference's -DPROFILING
+ * build (src/hybrid/infoli.h:35-36, src/hybrid/infoli.c:637-643,974-1000),
+ * which accumulates per-phase wall times.  When enabled, thread 0 of every
+ * CTA accumulates global-timer intervals per step: [0] tile staging wait,
+ * [1] gap-junction coupling, [2] compartment update (until the whole CTA is
+ * done), [3] grid barrier.  get_profile reports ns per step, averaged over
+ * CTAs (mean_ns) and the slowest CTA (max_ns), since profiling was enabled. */
+int infoli_sim_set_profiling(infoli_sim* s, int on);
+int infoli_sim_get_profile(infoli_sim* s, double mean_ns[4], double max_ns[4]);
+
+int infoli_sim_destroy(infoli_sim* s);
+
+/* ------------------------------------------------------------------------ */
+/* trace text (host side)                                                    */
+/* ------------------------------------------------------------------------ */
+
+/* "%.8f" of one float (promoted to double), byte-identical to the C
+ * library's printf; out needs 64 bytes.  Returns the length. */
+int infoli_format_f8(char* out, float v);
+
+/* One row of the reference's trace file (src/openmp/infoli.c:684-695):
+ * tagged != 0 gives "%d : %.8f " per cell with 1-based ids (normal build),
+ * tagged == 0 gives "%.8f " per cell (regression build); then "\n".
+ * Formats with up to nthreads threads (<= 0: all).  Returns bytes written or
+ * -1 when cap is too small (40 * n + 2 bytes always suffice). */
+int64_t infoli_format_row(char* buf, int64_t cap, const float* values, int n, int tagged, int nthreads);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* INFOLI_GPU_H */

@@ -1,0 +1,325 @@
+"""ctypes binding of libinfoli_gpu.so (include/infoli_gpu.h).
+
+This is the Python side of the drop-in boundary: it calls exactly the C entry
+points a C host (infoli.x) or any other FFI would call.  There is no CPU
+fallback: if the shared library is missing the import fails loudly, and every
+GPU entry point reports the CUDA error of the box it runs on.
+"""
+from __future__ import annotations
+
+import ctypes as C
+import os
+
+import numpy as np
+
+_HERE = os.path.dirname(os.path.abspath(__file__))
+LIB_PATH = os.path.join(_HERE, "_build", "libinfoli_gpu.so")
+
+NPARAM = 23
+NSTATE = 19
+NCONF = 42
+TRACE_AXON, TRACE_SOMA, TRACE_DEND = 1, 2, 4
+F_KAHAN = 1
+
+OK = 0
+ERR_ARG, ERR_CUDA, ERR_NOMEM, ERR_TIMEOUT = -1, -2, -3, -4
+ERR_FILE, ERR_CONFIG, ERR_CAPACITY, ERR_STATE = -5, -6, -7, -8
+
+STATE_NAMES = [
+    "V_dend", "Calcium_r", "Potassium_s", "Hcurrent_q", "Ca2Plus", "I_CaH", "g_CaL",
+    "V_soma", "Sodium_m", "Sodium_h", "Potassium_n", "Potassium_p", "Potassium_x_s",
+    "Calcium_k", "Calcium_l", "V_axon", "Sodium_m_a", "Sodium_h_a", "Potassium_x_a",
+]
+S = {name: i for i, name in enumerate(STATE_NAMES)}
+
+# Every symbol the header declares; tests check the library exports all of them.
+EXPORTED = [
+    "infoli_last_error", "infoli_version", "infoli_build_info", "infoli_device_count",
+    "infoli_read_parameters", "infoli_read_gcal", "infoli_gen_uniform", "infoli_gen_grid_gaussian",
+    "infoli_gen_fixed_degree", "infoli_bitmask_to_csr", "infoli_sim_create",
+    "infoli_sim_set_stimulus_pulse", "infoli_sim_set_stimulus_cells", "infoli_sim_run",
+    "infoli_sim_run_into", "infoli_sim_get_state", "infoli_sim_set_state", "infoli_sim_step",
+    "infoli_sim_last_run_stats", "infoli_sim_plan_info", "infoli_sim_destroy", "infoli_format_f8",
+    "infoli_format_row", "infoli_sim_set_profiling", "infoli_sim_get_profile",
+]
+
+
+class InfoliError(RuntimeError):
+    def __init__(self, code: int, msg: str):
+        super().__init__(f"infoli error {code}: {msg}")
+        self.code = code
+
+
+class SimDesc(C.Structure):
+    _fields_ = [
+        ("n_cells", C.c_int),
+        ("params", C.c_void_p),
+        ("init_state", C.c_void_p),
+        ("init_values", C.c_void_p),
+        ("row_ptr", C.c_void_p),
+        ("col", C.c_void_p),
+        ("g", C.c_void_p),
+        ("g_uniform", C.c_float),
+        ("flags", C.c_int),
+        ("device", C.c_int),
+    ]
+
+
+TRACE_CB = C.CFUNCTYPE(None, C.c_void_p, C.c_int, C.c_int, C.POINTER(C.c_float), C.c_int)
+
+_lib = None
+
+
+def load():
+    """Load libinfoli_gpu.so (raises if it has not been built)."""
+    global _lib
+    if _lib is not None:
+        return _lib
+    if not os.path.exists(LIB_PATH):
+        raise ImportError(f"{LIB_PATH} is missing: build it with `python -m infoli_gb300.build`")
+    L = C.CDLL(LIB_PATH)
+    P, I, I64, F, U = C.c_void_p, C.c_int, C.c_int64, C.c_float, C.c_uint
+    sig = {
+        "infoli_last_error": ([], C.c_char_p),
+        "infoli_version": ([], I),
+        "infoli_build_info": ([], C.c_char_p),
+        "infoli_device_count": ([], I),
+        "infoli_read_parameters": ([C.c_char_p, P], I),
+        "infoli_read_gcal": ([C.c_char_p, I, P], I),
+        "infoli_gen_uniform": ([I, F, U, P, P, I64, P], I),
+        "infoli_gen_grid_gaussian": ([I, I, F, F, C.c_uint64, P, P, I64, P], I),
+        "infoli_gen_fixed_degree": ([I, I, F, F, C.c_uint64, P, P, P, I64], I),
+        "infoli_bitmask_to_csr": ([I, P, P, P, I64, P], I),
+        "infoli_sim_create": ([C.POINTER(SimDesc), C.POINTER(C.c_void_p)], I),
+        "infoli_sim_set_stimulus_pulse": ([P, I, I, F], I),
+        "infoli_sim_set_stimulus_cells": ([P, P, P, I], I),
+        "infoli_sim_run": ([P, I, I, I, TRACE_CB, P], I),
+        "infoli_sim_run_into": ([P, I, I, I, P, I64, P], I),
+        "infoli_sim_get_state": ([P, P], I),
+        "infoli_sim_set_state": ([P, P], I),
+        "infoli_sim_step": ([P, P], I),
+        "infoli_sim_last_run_stats": ([P, P, P], I),
+        "infoli_sim_plan_info": ([P, P, P, P, P, P], I),
+        "infoli_sim_destroy": ([P], I),
+        "infoli_sim_set_profiling": ([P, I], I),
+        "infoli_sim_get_profile": ([P, P, P], I),
+        "infoli_format_f8": ([C.c_char_p, F], I),
+        "infoli_format_row": ([C.c_char_p, I64, P, I, I, I], I64),
+    }
+    for name, (args, res) in sig.items():
+        fn = getattr(L, name)
+        fn.argtypes = args
+        fn.restype = res
+    _lib = L
+    return L
+
+
+def _p(a):
+    return None if a is None else a.ctypes.data_as(C.c_void_p)
+
+
+def _check(rc):
+    if rc < 0:
+        raise InfoliError(rc, load().infoli_last_error().decode(errors="replace"))
+    return rc
+
+
+# ---------------------------------------------------------------- host side --
+
+def read_parameters(path: str) -> np.ndarray:
+    v = np.zeros(NCONF, dtype=np.float32)
+    _check(load().infoli_read_parameters(os.fsencode(path), _p(v)))
+    return v
+
+
+def read_gcal(path: str, g_cal: np.ndarray) -> int:
+    assert g_cal.dtype == np.float32 and g_cal.flags.c_contiguous
+    return _check(load().infoli_read_gcal(os.fsencode(path), g_cal.size, _p(g_cal)))
+
+
+def _csr_call(fn, n, *args, cap_hint):
+    row_ptr = np.zeros(n + 1, dtype=np.int64)
+    cap = max(16, int(cap_hint))
+    ne = C.c_int64(0)
+    while True:
+        col = np.zeros(cap, dtype=np.int32)
+        rc = fn(*args, _p(row_ptr), _p(col), cap, C.byref(ne))
+        if rc == ERR_CAPACITY:
+            cap = int(ne.value)
+            continue
+        _check(rc)
+        return row_ptr, col[: ne.value].copy()
+
+
+def gen_uniform(n: int, p: float, seed: int):
+    """The reference's built-in generator (src/openmp/infoli.c:337-375)."""
+    L = load()
+    return _csr_call(L.infoli_gen_uniform, n, n, float(np.float32(p)), int(seed) & 0xFFFFFFFF,
+                     cap_hint=n * (n - 1) * min(1.0, float(p) * 1.1 + 0.01) + 64)
+
+
+def gen_grid_gaussian(rows: int, cols: int, sigma: float, radius: float, seed: int):
+    L = load()
+    cand = rows * cols * (3.2 * radius * radius + 8)
+    return _csr_call(L.infoli_gen_grid_gaussian, rows * cols, rows, cols, float(sigma), float(radius),
+                     int(seed) & (2**64 - 1), cap_hint=cand)
+
+
+def gen_fixed_degree(n: int, k: int, seed: int, g_range=None):
+    row_ptr = np.zeros(n + 1, dtype=np.int64)
+    col = np.zeros(n * k, dtype=np.int32)
+    g = np.zeros(n * k, dtype=np.float32) if g_range is not None else None
+    lo, hi = g_range if g_range is not None else (0.0, 0.0)
+    _check(load().infoli_gen_fixed_degree(n, k, float(lo), float(hi), int(seed) & (2**64 - 1),
+                                          _p(row_ptr), _p(col), _p(g), n * k))
+    return row_ptr, col, g
+
+
+def bitmask_to_csr(n: int, bits: np.ndarray):
+    bits = np.ascontiguousarray(bits, dtype=np.uint32)
+    assert bits.size == n * ((n + 31) // 32)
+    L = load()
+    return _csr_call(L.infoli_bitmask_to_csr, n, n, _p(bits), cap_hint=int(np.unpackbits(
+        bits.view(np.uint8)).sum()) + 16)
+
+
+def format_f8(v: float) -> str:
+    buf = C.create_string_buffer(64)
+    k = load().infoli_format_f8(buf, float(v))
+    return buf.raw[:k].decode()
+
+
+def format_row(values: np.ndarray, tagged: bool, nthreads: int = 0) -> str:
+    v = np.ascontiguousarray(values, dtype=np.float32)
+    cap = 40 * v.size + 64
+    buf = C.create_string_buffer(cap)
+    k = _check(load().infoli_format_row(buf, cap, _p(v), v.size, int(bool(tagged)), nthreads))
+    return buf.raw[:k].decode()
+
+
+def device_count() -> int:
+    return _check(load().infoli_device_count())
+
+
+# --------------------------------------------------------------- simulation --
+
+class Simulation:
+    """One network on the GPU (infoli_sim_* handle)."""
+
+    def __init__(self, n, params, row_ptr, col, g=None, g_uniform=None, init_state=None,
+                 init_values=None, kahan=False, device=0):
+        L = load()
+        self._L = L
+        params = np.ascontiguousarray(params, dtype=np.float32)
+        assert params.size >= NPARAM
+        self.params = params[:NPARAM].copy()
+        self.n = int(n)
+        self.row_ptr = np.ascontiguousarray(row_ptr, dtype=np.int64)
+        self.col = np.ascontiguousarray(col, dtype=np.int32)
+        self.g = None if g is None else np.ascontiguousarray(g, dtype=np.float32)
+        d = SimDesc()
+        d.n_cells = self.n
+        d.params = _p(self.params)
+        st = None
+        iv = None
+        if init_state is not None:
+            st = np.ascontiguousarray(init_state, dtype=np.float32).reshape(NSTATE, self.n)
+            d.init_state = _p(st)
+        else:
+            iv = np.ascontiguousarray(init_values, dtype=np.float32)
+            assert iv.size == NSTATE
+            d.init_values = _p(iv)
+        d.row_ptr = _p(self.row_ptr)
+        d.col = _p(self.col) if self.col.size else None
+        d.g = _p(self.g)
+        d.g_uniform = float(self.params[1] if g_uniform is None else g_uniform)
+        d.flags = F_KAHAN if kahan else 0
+        d.device = int(device)
+        h = C.c_void_p()
+        _check(L.infoli_sim_create(C.byref(d), C.byref(h)))
+        self._h = h
+
+    def close(self):
+        if getattr(self, "_h", None):
+            self._L.infoli_sim_destroy(self._h)
+            self._h = None
+
+    __del__ = close
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *exc):
+        self.close()
+
+    def set_stimulus_pulse(self, start, end, amp):
+        _check(self._L.infoli_sim_set_stimulus_pulse(self._h, int(start), int(end), float(amp)))
+
+    def set_stimulus_cells(self, amp, onset, duration):
+        self._amp = np.ascontiguousarray(amp, dtype=np.float32)
+        self._onset = np.ascontiguousarray(onset, dtype=np.int32)
+        _check(self._L.infoli_sim_set_stimulus_cells(self._h, _p(self._amp), _p(self._onset),
+                                                     int(duration)))
+
+    @property
+    def step(self) -> int:
+        v = C.c_int(0)
+        _check(self._L.infoli_sim_step(self._h, C.byref(v)))
+        return v.value
+
+    def run(self, n_steps, trace_every=0, what=TRACE_AXON):
+        """Advance n_steps; returns {"axon"/"soma"/"dend": [rows, n]} for the selected quantities."""
+        names = [nm for bit, nm in ((TRACE_AXON, "axon"), (TRACE_SOMA, "soma"), (TRACE_DEND, "dend"))
+                 if what & bit]
+        if trace_every <= 0:
+            _check(self._L.infoli_sim_run_into(self._h, int(n_steps), 0, 0, None, 0, None))
+            return {}
+        s0 = self.step
+        rows = sum(1 for t in range(s0, s0 + n_steps) if t % trace_every == 0)
+        out = np.zeros((max(rows, 1), len(names), self.n), dtype=np.float32)
+        got = C.c_int(0)
+        _check(self._L.infoli_sim_run_into(self._h, int(n_steps), int(trace_every), int(what), _p(out),
+                                           out.size, C.byref(got)))
+        assert got.value == rows
+        return {nm: out[:rows, i, :].copy() for i, nm in enumerate(names)}
+
+    def run_with_callback(self, n_steps, trace_every, what, fn):
+        """fn(step, what_bit, values[n]) per recorded quantity, in step order."""
+        def _cb(user, step, w, values, n):
+            fn(step, w, np.ctypeslib.as_array(values, shape=(n,)))
+        cb = TRACE_CB(_cb)
+        _check(self._L.infoli_sim_run(self._h, int(n_steps), int(trace_every), int(what), cb, None))
+
+    def get_state(self) -> np.ndarray:
+        out = np.zeros((NSTATE, self.n), dtype=np.float32)
+        _check(self._L.infoli_sim_get_state(self._h, _p(out)))
+        return out
+
+    def set_state(self, st):
+        st = np.ascontiguousarray(st, dtype=np.float32).reshape(NSTATE, self.n)
+        _check(self._L.infoli_sim_set_state(self._h, _p(st)))
+
+    def last_run_stats(self):
+        ms = C.c_float(0)
+        nl = C.c_int(0)
+        _check(self._L.infoli_sim_last_run_stats(self._h, C.byref(ms), C.byref(nl)))
+        return ms.value, nl.value
+
+    def set_profiling(self, on=True):
+        _check(self._L.infoli_sim_set_profiling(self._h, int(bool(on))))
+
+    def get_profile(self):
+        """{"mean"/"max": {"stage","couple","update","barrier"}: ns per step}."""
+        mean = np.zeros(4)
+        mx = np.zeros(4)
+        _check(self._L.infoli_sim_get_profile(self._h, _p(mean), _p(mx)))
+        keys = ("stage", "couple", "update", "barrier")
+        return {"mean": dict(zip(keys, mean.tolist())), "max": dict(zip(keys, mx.tolist()))}
+
+    def plan_info(self):
+        g, t, ti, ch = C.c_int(), C.c_int(), C.c_int(), C.c_int()
+        sm = C.c_int64()
+        _check(self._L.infoli_sim_plan_info(self._h, C.byref(g), C.byref(t), C.byref(ti), C.byref(ch),
+                                            C.byref(sm)))
+        return {"grid": g.value, "threads": t.value, "tiles": ti.value, "chunks": ch.value,
+                "smem_bytes": sm.value}

@@ -1,0 +1,597 @@
+// C ABI of libinfoli_gpu.so: simulation handles, device memory, the chunked
+// launch loop and trace streaming (pinned host slots filled by
+// cudaMemcpyAsync on a side stream while the next chunk of steps computes).
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <cstdio>
+#include <cstdlib>
+#include <cstring>
+#include <string>
+#include <vector>
+
+#include "../../include/infoli_gpu.h"
+#include "infoli_internal.h"
+#include "infoli_kernels.cuh"
+#include "infoli_planner.h"
+
+using namespace infoli;
+
+#define CK(call)                                                                                    \
+  do {                                                                                              \
+    cudaError_t e_ = (call);                                                                        \
+    if (e_ != cudaSuccess)                                                                          \
+      return infoli__fail(INFOLI_ERR_CUDA, "%s failed: %s (%s:%d)", #call, cudaGetErrorString(e_), \
+                          __FILE__, __LINE__);                                                      \
+  } while (0)
+
+namespace {
+
+constexpr int kThreads = 1024;
+constexpr int kMaxStepsPerLaunch = 8192;
+constexpr size_t kTraceSlotBytes = 64u << 20;
+
+unsigned long long wait_timeout_ns() {
+  const char* s = getenv("INFOLI_WAIT_TIMEOUT_MS");
+  long ms = s ? atol(s) : 4000;
+  if (ms <= 0) ms = 4000;
+  return (unsigned long long)ms * 1000000ull;
+}
+
+template <class T>
+int dev_upload(T** dst, const T* src, size_t count) {
+  *dst = nullptr;
+  if (count == 0) return INFOLI_OK;
+  CK(cudaMalloc((void**)dst, count * sizeof(T)));
+  CK(cudaMemcpy(*dst, src, count * sizeof(T), cudaMemcpyHostToDevice));
+  return INFOLI_OK;
+}
+
+}  // namespace
+
+struct infoli_sim {
+  int device = 0;
+  int n = 0;
+  int n_pad = 0;
+  ModelParams P{};
+  float g_uniform = 0.04f;
+  int kahan = 0;
+  int step = 0;
+  // plan
+  Plan plan;
+  CtaWork* d_cta = nullptr;
+  TileDesc* d_tiles = nullptr;
+  ChunkDesc* d_chunks = nullptr;
+  CellSlots* d_cell_slots = nullptr;
+  uint16_t* d_edges = nullptr;
+  float* d_edge_g = nullptr;
+  // state
+  float* d_vd[2] = {nullptr, nullptr};
+  float* d_st = nullptr;
+  double* d_ca = nullptr;
+  // stimulus
+  int stim_kind = STIM_PULSE;
+  int stim_start = 20000, stim_end = 20499;
+  float stim_amp = 6.0f;
+  float* d_cell_amp = nullptr;
+  int* d_cell_onset = nullptr;
+  int stim_dur = 0;
+  // sync
+  unsigned* d_bar = nullptr;
+  int* d_err = nullptr;
+  unsigned long long* d_prof = nullptr;  // per-CTA phase timers when profiling is on
+  // trace ring
+  float* d_trace[2] = {nullptr, nullptr};
+  float* h_trace[2] = {nullptr, nullptr};
+  size_t trace_slot_floats = 0;
+  cudaStream_t stream = nullptr, side = nullptr;
+  cudaEvent_t ev_kernel[2] = {nullptr, nullptr}, ev_copy[2] = {nullptr, nullptr};
+  cudaEvent_t ev_t0 = nullptr, ev_t1 = nullptr;
+  float last_ms = 0.0f;
+  int last_launches = 0;
+};
+
+namespace {
+
+void release(infoli_sim* s) {
+  if (!s) return;
+  cudaSetDevice(s->device);
+  if (s->stream) cudaStreamSynchronize(s->stream);
+  if (s->side) cudaStreamSynchronize(s->side);
+  void* dptrs[] = {s->d_cta,   s->d_tiles,  s->d_chunks, s->d_cell_slots, s->d_edges,
+                   s->d_edge_g, s->d_vd[0], s->d_vd[1],  s->d_st,         s->d_ca,
+                   s->d_cell_amp, s->d_cell_onset, s->d_bar, s->d_err, s->d_trace[0], s->d_trace[1],
+                   s->d_prof};
+  for (void* p : dptrs)
+    if (p) cudaFree(p);
+  for (float* h : s->h_trace)
+    if (h) cudaFreeHost(h);
+  for (cudaEvent_t e : {s->ev_kernel[0], s->ev_kernel[1], s->ev_copy[0], s->ev_copy[1], s->ev_t0, s->ev_t1})
+    if (e) cudaEventDestroy(e);
+  if (s->stream) cudaStreamDestroy(s->stream);
+  if (s->side) cudaStreamDestroy(s->side);
+  delete s;
+}
+
+// Map the 19 reference state arrays to device fields.
+const int kFieldOfState[INFOLI_NSTATE] = {
+    -1 /*V_dend -> vd*/, F_R, F_S, F_Q, -2 /*Ca2Plus -> ca*/, F_ICAH, F_GCAL, F_VS, F_M, F_H, F_N, F_P,
+    F_XS, F_K, F_L, F_VA, F_MA, F_HA, F_XA};
+
+int upload_state(infoli_sim* s, const float* state /*19 x n*/) {
+  const int n = s->n;
+  const size_t np = (size_t)s->n_pad;
+  std::vector<float> st((size_t)F_COUNT * np, 0.0f);
+  std::vector<double> ca(np, 0.0);
+  std::vector<float> vd(np, 0.0f);
+  for (int k = 0; k < INFOLI_NSTATE; ++k) {
+    const float* src = state + (size_t)k * n;
+    const int f = kFieldOfState[k];
+    if (f == -1)
+      std::copy(src, src + n, vd.begin());
+    else if (f == -2)
+      for (int c = 0; c < n; ++c) ca[c] = (double)src[c];
+    else
+      std::copy(src, src + n, st.begin() + (size_t)f * np);
+  }
+  CK(cudaMemcpy(s->d_st, st.data(), st.size() * sizeof(float), cudaMemcpyHostToDevice));
+  CK(cudaMemcpy(s->d_ca, ca.data(), ca.size() * sizeof(double), cudaMemcpyHostToDevice));
+  CK(cudaMemcpy(s->d_vd[s->step & 1], vd.data(), np * sizeof(float), cudaMemcpyHostToDevice));
+  CK(cudaMemcpy(s->d_vd[(s->step + 1) & 1], vd.data(), np * sizeof(float), cudaMemcpyHostToDevice));
+  return INFOLI_OK;
+}
+
+int fill_args(infoli_sim* s, StepArgs* a) {
+  std::memset(a, 0, sizeof *a);
+  a->P = s->P;
+  a->cta = s->d_cta;
+  a->tiles = s->d_tiles;
+  a->chunks = s->d_chunks;
+  a->cell_slots = reinterpret_cast<const int2*>(s->d_cell_slots);
+  a->edges = s->d_edges;
+  a->edge_g = s->d_edge_g;
+  a->cell_g = nullptr;
+  a->g_uniform = s->g_uniform;
+  a->vd[0] = s->d_vd[0];
+  a->vd[1] = s->d_vd[1];
+  a->st = s->d_st;
+  a->ca = s->d_ca;
+  a->n_pad = s->n_pad;
+  a->stim_kind = s->stim_kind;
+  a->stim_start = s->stim_start;
+  a->stim_end = s->stim_end;
+  a->stim_amp = s->stim_amp;
+  a->cell_amp = s->d_cell_amp;
+  a->cell_onset = s->d_cell_onset;
+  a->stim_dur = s->stim_dur;
+  a->bar = s->d_bar;
+  a->err = s->d_err;
+  a->timeout_ns = wait_timeout_ns();
+  a->shape = s->plan.shape;
+  a->prof = s->d_prof;
+  return INFOLI_OK;
+}
+
+int count_rows(int step0, int n_steps, int every) {
+  if (every <= 0 || n_steps <= 0) return 0;
+  // multiples of `every` in [step0, step0 + n_steps)
+  const long long hi = (long long)step0 + n_steps - 1;
+  const long long first = ((long long)step0 + every - 1) / every;
+  const long long last = hi / every;
+  return last >= first ? (int)(last - first + 1) : 0;
+}
+
+int nq_of(int what) { return !!(what & INFOLI_TRACE_AXON) + !!(what & INFOLI_TRACE_SOMA) + !!(what & INFOLI_TRACE_DEND); }
+
+int check_device_error(infoli_sim* s) {
+  int err = 0;
+  CK(cudaMemcpy(&err, s->d_err, sizeof(int), cudaMemcpyDeviceToHost));
+  if (err != DEV_OK) {
+    cudaMemset(s->d_err, 0, sizeof(int));
+    return infoli__fail(INFOLI_ERR_TIMEOUT, "device wait gave up (code %d): %s", err,
+                        err == DEV_ERR_BARRIER_TIMEOUT ? "grid barrier timeout" : "tile copy timeout");
+  }
+  return INFOLI_OK;
+}
+
+}  // namespace
+
+extern "C" {
+
+const char* infoli_build_info(void) {
+  return "libinfoli_gpu: sm_103a persistent cooperative step kernel, bulk-async (TMA) V_dend tiles, "
+         "FP32 coupling with SFU exp2, FP64 Ca2+";
+}
+
+int infoli_device_count(void) {
+  int n = 0;
+  cudaError_t e = cudaGetDeviceCount(&n);
+  if (e != cudaSuccess) return infoli__fail(INFOLI_ERR_CUDA, "cudaGetDeviceCount: %s", cudaGetErrorString(e));
+  return n;
+}
+
+int infoli_sim_create(const infoli_sim_desc* d, infoli_sim** out) {
+  infoli__clear_error();
+  if (!d || !out) return infoli__fail(INFOLI_ERR_ARG, "sim_create: null argument");
+  *out = nullptr;
+  if (d->n_cells <= 0) return infoli__fail(INFOLI_ERR_ARG, "sim_create: n_cells must be positive");
+  if (!d->params) return infoli__fail(INFOLI_ERR_ARG, "sim_create: params is NULL");
+  if (!d->init_state && !d->init_values)
+    return infoli__fail(INFOLI_ERR_ARG, "sim_create: need init_state or init_values");
+  if (!d->row_ptr) return infoli__fail(INFOLI_ERR_ARG, "sim_create: row_ptr is NULL");
+  int ndev = 0;
+  if (cudaGetDeviceCount(&ndev) != cudaSuccess || ndev <= 0)
+    return infoli__fail(INFOLI_ERR_CUDA, "sim_create: no CUDA device available");
+  if (d->device < 0 || d->device >= ndev) return infoli__fail(INFOLI_ERR_ARG, "sim_create: bad device %d", d->device);
+
+  infoli_sim* s = new infoli_sim();
+  s->device = d->device;
+  s->n = d->n_cells;
+  s->n_pad = pad_cells(d->n_cells);
+  s->g_uniform = d->g_uniform;
+  s->kahan = (d->flags & INFOLI_F_KAHAN) ? 1 : 0;
+  static_assert(sizeof(ModelParams) == INFOLI_NPARAM * sizeof(float), "param layout");
+  std::memcpy(&s->P, d->params, sizeof(ModelParams));
+
+  auto fail = [&](int rc) {
+    release(s);
+    return rc;
+  };
+  if (cudaSetDevice(s->device) != cudaSuccess) return fail(infoli__fail(INFOLI_ERR_CUDA, "cudaSetDevice failed"));
+
+  // ---- plan
+  int nsm = 0, smem_optin = 0;
+  cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, s->device);
+  cudaDeviceGetAttribute(&smem_optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, s->device);
+  PlanInput pin;
+  pin.n = s->n;
+  pin.row_ptr = d->row_ptr;
+  pin.col = d->col;
+  pin.g = d->g;
+  pin.grid = 0;
+  const char* gs = getenv("INFOLI_GRID");
+  if (gs) pin.grid = atoi(gs);
+  pin.grid_max = nsm;  // one 1024-thread CTA per SM
+  pin.threads = kThreads;
+  pin.smem_budget = (size_t)smem_optin - 1024;  // static shared (abort flag) headroom
+  pin.kahan = s->kahan;
+  pin.no_resident = getenv("INFOLI_NO_RESIDENT") ? 1 : 0;
+  std::string perr;
+  if (!make_plan(pin, &s->plan, &perr)) return fail(infoli__fail(INFOLI_ERR_ARG, "%s", perr.c_str()));
+  const int cores = max_coresident_ctas(kThreads, s->plan.smem_bytes);
+  if (cores < s->plan.grid)
+    return fail(infoli__fail(INFOLI_ERR_CUDA, "plan needs %d co-resident CTAs, device allows %d", s->plan.grid, cores));
+
+  int rc;
+  if ((rc = dev_upload(&s->d_cta, s->plan.cta.data(), s->plan.cta.size())) ||
+      (rc = dev_upload(&s->d_tiles, s->plan.tiles.data(), s->plan.tiles.size())) ||
+      (rc = dev_upload(&s->d_chunks, s->plan.chunks.data(), s->plan.chunks.size())) ||
+      (rc = dev_upload(&s->d_cell_slots, s->plan.cell_slots.data(), s->plan.cell_slots.size())) ||
+      (rc = dev_upload(&s->d_edges, s->plan.edges.data(), s->plan.edges.size())) ||
+      (rc = dev_upload(&s->d_edge_g, s->plan.edge_g.data(), s->plan.edge_g.size())))
+    return fail(rc);
+  // the kernel needs valid pointers even for empty tables
+  if (!s->d_chunks && cudaMalloc((void**)&s->d_chunks, sizeof(ChunkDesc)) != cudaSuccess)
+    return fail(infoli__fail(INFOLI_ERR_NOMEM, "cudaMalloc"));
+  if (!s->d_tiles && cudaMalloc((void**)&s->d_tiles, sizeof(TileDesc)) != cudaSuccess)
+    return fail(infoli__fail(INFOLI_ERR_NOMEM, "cudaMalloc"));
+  if (!s->d_edges && cudaMalloc((void**)&s->d_edges, 16) != cudaSuccess)
+    return fail(infoli__fail(INFOLI_ERR_NOMEM, "cudaMalloc"));
+
+  const size_t np = (size_t)s->n_pad;
+  if (cudaMalloc((void**)&s->d_vd[0], np * sizeof(float)) != cudaSuccess ||
+      cudaMalloc((void**)&s->d_vd[1], np * sizeof(float)) != cudaSuccess ||
+      cudaMalloc((void**)&s->d_st, (size_t)F_COUNT * np * sizeof(float)) != cudaSuccess ||
+      cudaMalloc((void**)&s->d_ca, np * sizeof(double)) != cudaSuccess ||
+      cudaMalloc((void**)&s->d_bar, 128) != cudaSuccess || cudaMalloc((void**)&s->d_err, 128) != cudaSuccess)
+    return fail(infoli__fail(INFOLI_ERR_NOMEM, "sim_create: device allocation failed"));
+  cudaMemset(s->d_vd[0], 0, np * sizeof(float));
+  cudaMemset(s->d_vd[1], 0, np * sizeof(float));
+  cudaMemset(s->d_err, 0, 128);
+  cudaMemset(s->d_bar, 0, 128);
+
+  std::vector<float> init;
+  const float* st = d->init_state;
+  if (!st) {
+    init.resize((size_t)INFOLI_NSTATE * s->n);
+    for (int k = 0; k < INFOLI_NSTATE; ++k)
+      std::fill(init.begin() + (size_t)k * s->n, init.begin() + (size_t)(k + 1) * s->n, d->init_values[k]);
+    st = init.data();
+  }
+  if ((rc = upload_state(s, st))) return fail(rc);
+
+  if (cudaStreamCreateWithFlags(&s->stream, cudaStreamNonBlocking) != cudaSuccess ||
+      cudaStreamCreateWithFlags(&s->side, cudaStreamNonBlocking) != cudaSuccess)
+    return fail(infoli__fail(INFOLI_ERR_CUDA, "stream creation failed"));
+  for (int i = 0; i < 2; ++i)
+    if (cudaEventCreateWithFlags(&s->ev_kernel[i], cudaEventDisableTiming) != cudaSuccess ||
+        cudaEventCreateWithFlags(&s->ev_copy[i], cudaEventDisableTiming) != cudaSuccess)
+      return fail(infoli__fail(INFOLI_ERR_CUDA, "event creation failed"));
+  if (cudaEventCreate(&s->ev_t0) != cudaSuccess || cudaEventCreate(&s->ev_t1) != cudaSuccess)
+    return fail(infoli__fail(INFOLI_ERR_CUDA, "event creation failed"));
+  *out = s;
+  return INFOLI_OK;
+}
+
+int infoli_sim_destroy(infoli_sim* s) {
+  infoli__clear_error();
+  release(s);
+  return INFOLI_OK;
+}
+
+int infoli_sim_set_stimulus_pulse(infoli_sim* s, int start_step, int end_step, float amp) {
+  infoli__clear_error();
+  if (!s) return infoli__fail(INFOLI_ERR_ARG, "null handle");
+  s->stim_kind = STIM_PULSE;
+  s->stim_start = start_step;
+  s->stim_end = end_step;
+  s->stim_amp = amp;
+  return INFOLI_OK;
+}
+
+int infoli_sim_set_stimulus_cells(infoli_sim* s, const float* amp, const int* onset, int duration) {
+  infoli__clear_error();
+  if (!s || !amp || !onset || duration < 0) return infoli__fail(INFOLI_ERR_ARG, "set_stimulus_cells: bad argument");
+  CK(cudaSetDevice(s->device));
+  if (!s->d_cell_amp) {
+    CK(cudaMalloc((void**)&s->d_cell_amp, (size_t)s->n_pad * sizeof(float)));
+    CK(cudaMalloc((void**)&s->d_cell_onset, (size_t)s->n_pad * sizeof(int)));
+    CK(cudaMemset(s->d_cell_amp, 0, (size_t)s->n_pad * sizeof(float)));
+    CK(cudaMemset(s->d_cell_onset, 0, (size_t)s->n_pad * sizeof(int)));
+  }
+  CK(cudaMemcpy(s->d_cell_amp, amp, (size_t)s->n * sizeof(float), cudaMemcpyHostToDevice));
+  CK(cudaMemcpy(s->d_cell_onset, onset, (size_t)s->n * sizeof(int), cudaMemcpyHostToDevice));
+  s->stim_kind = STIM_CELL;
+  s->stim_dur = duration;
+  return INFOLI_OK;
+}
+
+int infoli_sim_run(infoli_sim* s, int n_steps, int trace_every, int trace_what, infoli_trace_cb cb, void* user) {
+  infoli__clear_error();
+  if (!s || n_steps < 0) return infoli__fail(INFOLI_ERR_ARG, "sim_run: bad argument");
+  if (trace_every > 0 && (!cb || nq_of(trace_what) == 0))
+    return infoli__fail(INFOLI_ERR_ARG, "sim_run: tracing needs a callback and at least one quantity");
+  CK(cudaSetDevice(s->device));
+  const int nq = trace_every > 0 ? nq_of(trace_what) : 0;
+  const size_t row_floats = (size_t)nq * s->n_pad;
+
+  // launch length: bounded by kMaxStepsPerLaunch and by the trace slot size
+  int launch_steps = std::min(std::max(n_steps, 1), kMaxStepsPerLaunch);
+  if (nq > 0) {
+    const int rows_cap = (int)std::max<size_t>(1, kTraceSlotBytes / (row_floats * sizeof(float)));
+    launch_steps = std::min<long long>(launch_steps, (long long)rows_cap * trace_every);
+    const size_t need = (size_t)rows_cap * row_floats;
+    const int rows_needed = count_rows(0, launch_steps + trace_every, trace_every) + 1;
+    const size_t want = std::min(need, (size_t)rows_needed * row_floats);
+    if (s->trace_slot_floats < want) {
+      for (int i = 0; i < 2; ++i) {
+        if (s->d_trace[i]) cudaFree(s->d_trace[i]);
+        if (s->h_trace[i]) cudaFreeHost(s->h_trace[i]);
+        s->d_trace[i] = nullptr;
+        s->h_trace[i] = nullptr;
+      }
+      for (int i = 0; i < 2; ++i) {
+        CK(cudaMalloc((void**)&s->d_trace[i], want * sizeof(float)));
+        CK(cudaMallocHost((void**)&s->h_trace[i], want * sizeof(float)));
+      }
+      s->trace_slot_floats = want;
+    }
+  }
+
+  StepArgs a;
+  fill_args(s, &a);
+  a.trace_every = trace_every > 0 ? trace_every : 0;
+  a.trace_mask = trace_what;
+  a.trace_nq = nq;
+
+  struct Pending {
+    int slot, step0, rows;
+  };
+  std::vector<Pending> pend;
+  int launches = 0;
+  CK(cudaEventRecord(s->ev_t0, s->stream));
+  int done = 0, li = 0;
+  auto drain = [&](const Pending& p) -> int {
+    CK(cudaEventSynchronize(s->ev_copy[p.slot]));
+    int row = 0;
+    for (int t = 0; t < n_steps && row < p.rows; ++t) {
+      (void)t;
+    }
+    // rows are the multiples of trace_every in the launch's step range
+    int st = ((p.step0 + trace_every - 1) / trace_every) * trace_every;
+    for (row = 0; row < p.rows; ++row, st += trace_every) {
+      const float* base = s->h_trace[p.slot] + (size_t)row * row_floats;
+      int qi = 0;
+      for (int bit : {INFOLI_TRACE_AXON, INFOLI_TRACE_SOMA, INFOLI_TRACE_DEND})
+        if (trace_what & bit) cb(user, st, bit, base + (size_t)(qi++) * s->n_pad, s->n);
+    }
+    return INFOLI_OK;
+  };
+  while (done < n_steps) {
+    const int len = std::min(launch_steps, n_steps - done);
+    const int slot = li & 1;
+    a.step0 = s->step + done;
+    a.n_steps = len;
+    a.trace = nq ? s->d_trace[slot] : nullptr;
+    const int rows = count_rows(a.step0, len, trace_every);
+    // the slot's previous contents must have been copied and consumed
+    if (pend.size() >= 2) {
+      int rc = drain(pend.front());
+      if (rc) return rc;
+      pend.erase(pend.begin());
+    }
+    CK(cudaMemsetAsync(s->d_bar, 0, sizeof(unsigned), s->stream));
+    CK(launch_step_kernel(a, s->plan.grid, s->plan.threads, s->stream));
+    ++launches;
+    if (rows > 0) {
+      CK(cudaEventRecord(s->ev_kernel[slot], s->stream));
+      CK(cudaStreamWaitEvent(s->side, s->ev_kernel[slot], 0));
+      CK(cudaMemcpyAsync(s->h_trace[slot], s->d_trace[slot], (size_t)rows * row_floats * sizeof(float),
+                         cudaMemcpyDeviceToHost, s->side));
+      CK(cudaEventRecord(s->ev_copy[slot], s->side));
+      pend.push_back({slot, a.step0, rows});
+    }
+    done += len;
+    ++li;
+  }
+  CK(cudaEventRecord(s->ev_t1, s->stream));
+  for (const Pending& p : pend) {
+    int rc = drain(p);
+    if (rc) return rc;
+  }
+  CK(cudaStreamSynchronize(s->stream));
+  CK(cudaGetLastError());
+  float ms = 0.0f;
+  CK(cudaEventElapsedTime(&ms, s->ev_t0, s->ev_t1));
+  s->last_ms = ms;
+  s->last_launches = launches;
+  int rc = check_device_error(s);
+  if (rc) return rc;
+  s->step += n_steps;
+  return INFOLI_OK;
+}
+
+namespace {
+struct IntoCtx {
+  float* out;
+  int64_t cap;
+  int n;
+  int nq;
+  int what;
+  int rows;
+  int last_step;
+  int overflow;
+};
+void into_cb(void* user, int step, int what, const float* values, int n) {
+  IntoCtx* c = (IntoCtx*)user;
+  if (step != c->last_step) {
+    c->last_step = step;
+    c->rows++;
+  }
+  int qi = 0;
+  for (int bit : {INFOLI_TRACE_AXON, INFOLI_TRACE_SOMA, INFOLI_TRACE_DEND}) {
+    if (!(c->what & bit)) continue;
+    if (bit == what) break;
+    ++qi;
+  }
+  const int64_t off = ((int64_t)(c->rows - 1) * c->nq + qi) * n;
+  if (off + n > c->cap) {
+    c->overflow = 1;
+    return;
+  }
+  std::memcpy(c->out + off, values, sizeof(float) * n);
+}
+}  // namespace
+
+int infoli_sim_run_into(infoli_sim* s, int n_steps, int trace_every, int trace_what, float* out,
+                        int64_t out_capacity_floats, int* rows_out) {
+  infoli__clear_error();
+  if (!s) return infoli__fail(INFOLI_ERR_ARG, "null handle");
+  if (trace_every <= 0) {
+    int rc = infoli_sim_run(s, n_steps, 0, 0, nullptr, nullptr);
+    if (rows_out) *rows_out = 0;
+    return rc;
+  }
+  if (!out) return infoli__fail(INFOLI_ERR_ARG, "run_into: out is NULL");
+  IntoCtx c{out, out_capacity_floats, s->n, nq_of(trace_what), trace_what, 0, -1, 0};
+  int rc = infoli_sim_run(s, n_steps, trace_every, trace_what, into_cb, &c);
+  if (rows_out) *rows_out = c.rows;
+  if (rc) return rc;
+  if (c.overflow) return infoli__fail(INFOLI_ERR_CAPACITY, "run_into: output buffer too small");
+  return INFOLI_OK;
+}
+
+int infoli_sim_get_state(infoli_sim* s, float* out) {
+  infoli__clear_error();
+  if (!s || !out) return infoli__fail(INFOLI_ERR_ARG, "get_state: bad argument");
+  CK(cudaSetDevice(s->device));
+  CK(cudaStreamSynchronize(s->stream));
+  const int n = s->n;
+  const size_t np = (size_t)s->n_pad;
+  std::vector<float> st((size_t)F_COUNT * np), vd(np);
+  std::vector<double> ca(np);
+  CK(cudaMemcpy(st.data(), s->d_st, st.size() * sizeof(float), cudaMemcpyDeviceToHost));
+  CK(cudaMemcpy(ca.data(), s->d_ca, ca.size() * sizeof(double), cudaMemcpyDeviceToHost));
+  CK(cudaMemcpy(vd.data(), s->d_vd[s->step & 1], np * sizeof(float), cudaMemcpyDeviceToHost));
+  for (int k = 0; k < INFOLI_NSTATE; ++k) {
+    float* dst = out + (size_t)k * n;
+    const int f = kFieldOfState[k];
+    if (f == -1)
+      std::copy(vd.begin(), vd.begin() + n, dst);
+    else if (f == -2)
+      for (int c = 0; c < n; ++c) dst[c] = (float)ca[c];
+    else
+      std::copy(st.begin() + (size_t)f * np, st.begin() + (size_t)f * np + n, dst);
+  }
+  return INFOLI_OK;
+}
+
+int infoli_sim_set_state(infoli_sim* s, const float* in) {
+  infoli__clear_error();
+  if (!s || !in) return infoli__fail(INFOLI_ERR_ARG, "set_state: bad argument");
+  CK(cudaSetDevice(s->device));
+  CK(cudaStreamSynchronize(s->stream));
+  return upload_state(s, in);
+}
+
+int infoli_sim_step(infoli_sim* s, int* step_out) {
+  if (!s || !step_out) return infoli__fail(INFOLI_ERR_ARG, "sim_step: bad argument");
+  *step_out = s->step;
+  return INFOLI_OK;
+}
+
+int infoli_sim_last_run_stats(infoli_sim* s, float* device_ms, int* launches) {
+  if (!s) return infoli__fail(INFOLI_ERR_ARG, "null handle");
+  if (device_ms) *device_ms = s->last_ms;
+  if (launches) *launches = s->last_launches;
+  return INFOLI_OK;
+}
+
+int infoli_sim_set_profiling(infoli_sim* s, int on) {
+  infoli__clear_error();
+  if (!s) return infoli__fail(INFOLI_ERR_ARG, "null handle");
+  CK(cudaSetDevice(s->device));
+  CK(cudaStreamSynchronize(s->stream));
+  if (!on) {
+    if (s->d_prof) cudaFree(s->d_prof);
+    s->d_prof = nullptr;
+    return INFOLI_OK;
+  }
+  const size_t bytes = (size_t)s->plan.grid * kProfSlots * sizeof(unsigned long long);
+  if (!s->d_prof) CK(cudaMalloc((void**)&s->d_prof, bytes));
+  CK(cudaMemset(s->d_prof, 0, bytes));
+  return INFOLI_OK;
+}
+
+int infoli_sim_get_profile(infoli_sim* s, double mean_ns[4], double max_ns[4]) {
+  infoli__clear_error();
+  if (!s || !s->d_prof) return infoli__fail(INFOLI_ERR_STATE, "profiling is not enabled");
+  CK(cudaSetDevice(s->device));
+  CK(cudaStreamSynchronize(s->stream));
+  std::vector<unsigned long long> h((size_t)s->plan.grid * kProfSlots);
+  CK(cudaMemcpy(h.data(), s->d_prof, h.size() * sizeof(unsigned long long), cudaMemcpyDeviceToHost));
+  for (int k = 0; k < 4; ++k) {
+    double sum = 0, mx = 0;
+    for (int b = 0; b < s->plan.grid; ++b) {
+      const unsigned long long steps = h[(size_t)b * kProfSlots + PROF_STEPS];
+      const double v = steps ? (double)h[(size_t)b * kProfSlots + k] / (double)steps : 0.0;
+      sum += v;
+      mx = std::max(mx, v);
+    }
+    if (mean_ns) mean_ns[k] = sum / std::max(1, s->plan.grid);
+    if (max_ns) max_ns[k] = mx;
+  }
+  return INFOLI_OK;
+}
+
+int infoli_sim_plan_info(infoli_sim* s, int* grid, int* threads, int* tiles, int* chunks, int64_t* smem_bytes) {
+  if (!s) return infoli__fail(INFOLI_ERR_ARG, "null handle");
+  if (grid) *grid = s->plan.grid;
+  if (threads) *threads = s->plan.threads;
+  if (tiles) *tiles = (int)s->plan.tiles.size();
+  if (chunks) *chunks = (int)s->plan.chunks.size();
+  if (smem_bytes) *smem_bytes = (int64_t)s->plan.smem_bytes;
+  return INFOLI_OK;
+}
+
+}  // extern "C"

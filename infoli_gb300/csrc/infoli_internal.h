@@ -1,0 +1,21 @@
+/* Internal helpers shared by the C and CUDA translation units of libinfoli_gpu.so. */
+#ifndef INFOLI_INTERNAL_H
+#define INFOLI_INTERNAL_H
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* Record a message for infoli_last_error() and return `code`. */
+int infoli__fail(int code, const char* fmt, ...)
+#ifdef __GNUC__
+    __attribute__((format(printf, 2, 3)))
+#endif
+    ;
+void infoli__clear_error(void);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif

@@ -1,0 +1,112 @@
+// Work decomposition shared by the host planner (infoli_plan.cpp) and the
+// persistent step kernel (infoli_kernels.cu).  Plain-old-data only.
+//
+// A network (or a batch of independent networks laid side by side) is a set
+// of receiver cells with CSR neighbour lists into one global V_dend array.
+// The planner cuts it into CTA work items:
+//   * a CTA owns a contiguous run of cells (<= its thread count); one thread
+//     per owned cell runs the fused compartment update, state in registers;
+//   * the senders its receivers read form one or more "tiles": contiguous,
+//     16-byte-aligned ranges of the V_dend array that are staged into shared
+//     memory by a bulk async copy each step;
+//   * the edges of a (receiver, tile) pair are cut into chunks of at most
+//     kChunkEdges; one warp reduces one chunk into one partial-sum slot; the
+//     update thread adds its receiver's slots in sender order.
+// Edge entries are 16-bit offsets from the tile start (a tile is at most
+// 65536 floats), so one gather from shared memory per edge.
+#pragma once
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+namespace infoli {
+#endif
+
+enum { kChunkEdges = 128 };
+
+typedef struct {
+  int cell_begin;   // first owned cell (index into the V_dend / state arrays)
+  int n_cells;      // owned cells, <= threads per CTA
+  int tile_begin;   // first tile of this CTA in the tile table
+  int n_tiles;      // tiles this CTA stages each step
+  int slot_begin;   // partial slots of this CTA: chunk ids slot_begin.. (absolute)
+  int n_slots;      // number of chunks == number of partial slots
+  int pad0, pad1;
+} CtaWork;
+
+typedef struct {
+  int lo;           // first V_dend index of the tile (multiple of 4)
+  int nfloats;      // tile length in floats (multiple of 4)
+  int chunk_begin;  // chunks of this tile: [chunk_begin, chunk_end), absolute
+  int chunk_end;
+} TileDesc;
+
+typedef struct {
+  int edge_begin;   // absolute index into the edge-offset (and per-edge g) arrays
+  int slot;         // partial slot, relative to the CTA's slot_begin
+  int recv;         // receiver, relative to the CTA's cell_begin
+  int count;        // edges in this chunk, 1..kChunkEdges
+} ChunkDesc;
+
+#if defined(__CUDACC__)
+#define INFOLI_HD __host__ __device__
+#else
+#define INFOLI_HD
+#endif
+
+// Sizes that fix the step kernel's dynamic shared memory.  When res_chunks
+// is non-zero the CTA's static work (tile and chunk descriptors, edge
+// offsets, per-edge conductances) is copied into shared memory once per
+// launch ("resident" plan) instead of being re-read from global memory
+// every step.
+typedef struct {
+  int tile_cap;    // floats per tile buffer
+  int nbuf;        // tile buffers (1 or 2)
+  int threads;     // threads per CTA
+  int max_slots;   // partial-sum slots per CTA
+  int kahan;       // compensated sums (second slot array)
+  int res_tiles;   // resident tile descriptors per CTA (0: not resident)
+  int res_chunks;  // resident chunk descriptors per CTA
+  int res_edges;   // resident edge offsets per CTA
+  int edge_g;      // per-edge conductances present
+} SmemShape;
+
+// Dynamic shared-memory layout of the step kernel (byte offsets):
+//   [tile buffers: nbuf x tile_cap floats][own V_dend: threads floats]
+//   [partial sums: max_slots floats][Kahan compensations: max_slots floats]
+//   [2 mbarriers, 16-byte aligned]
+//   resident plans only: [tile descs][chunk descs][per-edge g][edge offsets]
+typedef struct {
+  size_t tiles, vown, part, partc, mbar, tdesc, chunks, eg, edges, total;
+} SmemLayout;
+
+static inline INFOLI_HD SmemLayout smem_layout(SmemShape s) {
+  SmemLayout L;
+  size_t off = 0;
+  L.tiles = off;
+  off += (size_t)s.nbuf * (size_t)s.tile_cap * sizeof(float);
+  L.vown = off;
+  off += (size_t)s.threads * sizeof(float);
+  L.part = off;
+  off += (size_t)s.max_slots * sizeof(float);
+  L.partc = off;
+  if (s.kahan) off += (size_t)s.max_slots * sizeof(float);
+  off = (off + 15) & ~(size_t)15;
+  L.mbar = off;
+  off += 2 * sizeof(uint64_t);
+  L.tdesc = off;
+  off += (size_t)s.res_tiles * sizeof(TileDesc);
+  L.chunks = off;
+  off += (size_t)s.res_chunks * sizeof(ChunkDesc);
+  L.eg = off;
+  if (s.edge_g) off += (size_t)s.res_edges * sizeof(float);
+  L.edges = off;
+  off += (size_t)s.res_edges * sizeof(uint16_t);
+  off = (off + 15) & ~(size_t)15;
+  L.total = off;
+  return L;
+}
+
+#ifdef __cplusplus
+}  // namespace infoli
+#endif

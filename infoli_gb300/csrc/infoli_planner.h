@@ -1,0 +1,53 @@
+// Host planner: cuts a CSR network into the CTA / tile / chunk work items of
+// the persistent step kernel (see infoli_plan.h for the device-side view).
+#pragma once
+#include <cstddef>
+#include <cstdint>
+#include <string>
+#include <vector>
+
+#include "infoli_plan.h"
+
+namespace infoli {
+
+// Length of every per-cell device array for n cells: a multiple of 32 with
+// 32 spare entries, so tile ends rounded up to 16 bytes stay in bounds.
+inline int pad_cells(int n) { return ((n + 31) / 32) * 32 + 32; }
+
+struct alignas(8) CellSlots {
+  int begin;  // first partial slot, relative to the CTA
+  int count;  // number of slots (chunks) of this receiver
+};
+
+struct PlanInput {
+  int n = 0;                       // receivers 0..n-1 (also the sender id space)
+  const int64_t* row_ptr = nullptr;
+  const int32_t* col = nullptr;
+  const float* g = nullptr;        // per-edge conductance or null
+  int grid = 0;                    // CTAs to use (0: heuristic, capped by grid_max)
+  int grid_max = 0;                // co-resident CTA limit
+  int threads = 1024;              // threads per CTA
+  size_t smem_budget = 0;          // dynamic shared memory per CTA (bytes)
+  int kahan = 0;
+  int no_resident = 0;             // force per-step reads of the static work from global memory
+};
+
+struct Plan {
+  int grid = 0, threads = 0, tile_cap = 0, nbuf = 1, max_slots = 0;
+  SmemShape shape{};                  // shared-memory shape of the launch
+  size_t smem_bytes = 0;
+  std::vector<CtaWork> cta;
+  std::vector<TileDesc> tiles;
+  std::vector<ChunkDesc> chunks;
+  std::vector<CellSlots> cell_slots;  // [n]
+  std::vector<uint16_t> edges;
+  std::vector<float> edge_g;          // empty unless per-edge g
+};
+
+// Shared-memory bytes the step kernel needs for a plan's parameters.
+size_t plan_smem_bytes(int tile_cap, int nbuf, int threads, int max_slots, int kahan);
+
+// Returns false and sets *err on failure.
+bool make_plan(const PlanInput& in, Plan* out, std::string* err);
+
+}  // namespace infoli

@@ -1,0 +1,104 @@
+"""The CPU oracle is pinned to the untouched reference (golden fixtures made by
+tests/golden/make_golden.py from oracle/build_ref.sh's binaries)."""
+import numpy as np
+import pytest
+
+from helpers import CONF, golden, kat_topology, spike_steps
+from oracle import oracle as O
+
+
+@pytest.fixture(scope="module")
+def conf(built):
+    return O.read_parameters(CONF)
+
+
+def _fmt8(a):
+    return np.array([float("%.8f" % float(x)) for x in a.ravel()]).reshape(a.shape)
+
+
+def test_read_parameters_matches_reference_defaults(conf):
+    assert conf.shape == (42,)
+    assert conf[0] == np.float32(0.05) and conf[1] == np.float32(0.04)
+    assert conf[23] == -60 and conf[41] == np.float32(0.2369847)
+
+
+def test_generator_known_answer(built):
+    # seed-1 draws of the reference generator on 50 cells at p=0.3 (742 edges)
+    rp, col = O.gen_uniform(50, np.float32(0.3), 1)
+    assert rp[-1] == 742
+    for r in range(50):
+        row = col[rp[r]:rp[r + 1]]
+        assert np.all(np.diff(row) > 0) and r not in row
+
+
+def test_oracle_bit_exact_vs_reference_omp_test(conf):
+    """Generator + coupling + update, 50 cells, 500 steps: byte-identical trace text."""
+    z = golden("omp_test_n50_p0.3_t25.npz")
+    n = int(z["n"])
+    rp, col = O.gen_uniform(n, np.float32(z["p"]), int(z["seed"]))
+    st = O.default_state(n, conf)
+    st[O.S["g_CaL"]] = z["gcal"]
+    steps = int(np.float32(z["t"]) / conf[0])
+    tr = O.run(n, conf[:23], st, rp, col, g_uniform=conf[1], nsteps=steps, trace_every=1,
+               traces=("axon",))["axon"]
+    assert np.array_equal(_fmt8(tr), z["v_axon"])
+
+
+def test_oracle_bit_exact_through_spikes(conf):
+    """20 cells, 22000 steps with the 6 uA pulse: same rows and spike steps."""
+    z = golden("omp_test_n20_p0.5_t1100.npz")
+    n = int(z["n"])
+    rp, col = O.gen_uniform(n, np.float32(z["p"]), int(z["seed"]))
+    st = O.default_state(n, conf)
+    st[O.S["g_CaL"]] = z["gcal"]
+    steps = int(z["n_steps"])
+    tr = O.run(n, conf[:23], st, rp, col, g_uniform=conf[1], nsteps=steps, trace_every=1,
+               traces=("axon",))["axon"]
+    assert np.array_equal(_fmt8(tr[::10]), z["v_axon_every10"])
+    sp = spike_steps(tr)
+    for c in range(n):
+        assert np.array_equal(sp[c], z[f"spikes_{c}"])
+
+
+def test_oracle_trace_format_vs_reference_output(conf):
+    """Normal build output file (src/openmp/infoli.c:383-396,682-696): header, then
+    every 100th step ' %d %.2f ' + '%d : %.8f ' per cell; byte-identical rows."""
+    lines = open(__import__("os").path.join(__import__("helpers").GOLDEN, "omp_n200_p0.1_t30.txt")).read().split("\n")
+    n = 200
+    assert lines[2] == "#simSteps Input(Iapp) Output(V_axon)" + "".join("%d " % c for c in range(n))
+    st = O.default_state(n, conf)
+    rp, col = O.gen_uniform(n, np.float32(0.1), 1)
+    tr = O.run(n, conf[:23], st, rp, col, g_uniform=conf[1], nsteps=600, trace_every=100,
+               traces=("axon",))["axon"]
+    assert len(tr) == 6 and lines[9] == ""
+    for k, row in enumerate(tr):
+        want = " %d %.2f " % (100 * k + 1, 0.0) + "".join("%d : %.8f " % (c + 1, float(v)) for c, v in enumerate(row))
+        assert lines[3 + k] == want
+
+
+def test_kat_regression_checker_criterion(conf):
+    """The reference's own regression check (src/regression_test/regression_checker.c:41-65):
+    max relative error <= 1% over the 'standard' 500 ms, against stable_version.c's
+    golden; plus identical spike steps over the 'full' 2000 ms."""
+    n, rp, col, g, gcal = kat_topology()
+    z = golden("kat_stable_version.npz")
+    st = O.default_state(n, conf)
+    st[O.S["g_CaL"]] = gcal
+    steps = int(z["n_steps"])
+    tr = O.run(n, conf[:23], st, rp, col, g=g, nsteps=steps, trace_every=1, traces=("axon",))["axon"]
+    base = z["v_axon_first10000"]
+    assert np.max(np.abs(tr[:10000] - base) / np.abs(base)) <= 0.01
+    sp = spike_steps(tr)
+    for c in range(n):
+        assert np.array_equal(sp[c], z[f"spikes_{c}"])
+
+
+def test_fp64_twin_close_to_fp32(conf):
+    n, rp, col, g, gcal = kat_topology()
+    st32 = O.default_state(n, conf)
+    st32[O.S["g_CaL"]] = gcal
+    st64 = st32.astype(np.float64)
+    a = O.run(n, conf[:23], st32, rp, col, g=g, nsteps=2000, trace_every=1, traces=("soma",))["soma"]
+    b = O.run(n, conf[:23].astype(np.float64), st64, rp, col, g=g, nsteps=2000, trace_every=1,
+              traces=("soma",), fp64=True)["soma"]
+    assert np.max(np.abs(a - b)) < 1e-3
