@@ -1,0 +1,314 @@
+"""Benchmark: cell-steps/s of the InfOli network update on one GB300 (or N replicas).
+
+Workload (default): 10,000 cells on a 100x100 grid, Gaussian-distance
+connectivity (sigma = 10 cells, candidates within radius 18 = ~1,000 cells per
+receiver, mean degree ~439), uniform g = 0.04, initial V_dend = -60 + U(-1,1) mV
+and g_CaL ~ U(0.6, 0.8) from seed 1, the reference's 6 uA pulse schedule.
+One bench step = one infoli_sim_run call advancing 1,000 explicit-Euler
+timesteps (50 ms simulated) with the V_axon trace streamed to the host every
+100 timesteps, as the reference prints it.  40 bench steps = the 2 s run.
+
+  python bench.py [--gpus N] [--steps K] [--warmup W] [--impl gb300|reference]
+
+value: cells x timesteps / device time (CUDA events on the simulation's stream,
+state and topology resident in HBM).  e2e: the same work through the C ABI from
+host buffers: per bench step set_state (H2D), run with the trace (D2H), and
+get_state (D2H), wall-clock.  The reference arm times the CPU restatement of
+the reference's OpenMP loop (oracle/, C + OpenMP, all host cores) on a bounded
+sample of the same workload.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import threading
+import time
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+ROWS, COLS, SIGMA, RADIUS, SEED = 100, 100, 10.0, 18.0, 1
+STEPS_PER_ITER = 1000
+TRACE_EVERY = 100
+
+
+def peaks():
+    try:
+        with open(os.path.join(ROOT, "MEASURED_PEAKS.json")) as f:
+            d = json.load(f)
+        return float(d["hbm_gbs"]), "measured"
+    except Exception:
+        return 6800.0, "fallback"
+
+
+def workload():
+    import numpy as np
+
+    import infoli_gb300 as ig
+
+    conf = ig.read_parameters(os.path.join(ROOT, "infoli_gb300", "host", "default.conf"))
+    rp, col = ig.gen_grid_gaussian(ROWS, COLS, SIGMA, RADIUS, SEED)
+    n = ROWS * COLS
+    st = np.empty((19, n), dtype=np.float32)
+    st[:] = conf[23:42][:, None]
+    rng = np.random.default_rng(SEED)
+    st[0] += rng.uniform(-1, 1, n).astype(np.float32)
+    st[6] = rng.uniform(0.6, 0.8, n).astype(np.float32)
+    return conf, n, rp, col, st
+
+
+class ClockSampler:
+    """nvidia-smi clocks/throttle reasons sampled during the timed region."""
+
+    def __init__(self, index):
+        self.index = index
+        self.rows = []
+        self.proc = None
+
+    def __enter__(self):
+        q = ("clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.hw_slowdown,"
+             "clocks_event_reasons.hw_thermal_slowdown,clocks_event_reasons.sw_thermal_slowdown,"
+             "clocks_event_reasons.sw_power_cap")
+        try:
+            self.proc = subprocess.Popen(["nvidia-smi", "-i", str(self.index), f"--query-gpu={q}",
+                                          "--format=csv,noheader,nounits", "-lms", "100"],
+                                         stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self.thread = threading.Thread(target=self._read, daemon=True)
+            self.thread.start()
+        except Exception:
+            self.proc = None
+        return self
+
+    def _read(self):
+        for line in self.proc.stdout:
+            parts = [p.strip() for p in line.split(",")]
+            if len(parts) == 7:
+                self.rows.append(parts)
+
+    def __exit__(self, *exc):
+        if self.proc:
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=5)
+            except Exception:
+                self.proc.kill()
+
+    def summary(self):
+        if not self.rows:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["unsampled"], "samples": 0}
+        sm = [float(r[0]) for r in self.rows if r[0].replace(".", "").isdigit()]
+        mx = [float(r[1]) for r in self.rows if r[1].replace(".", "").isdigit()]
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        reasons = sorted({names[i] for r in self.rows for i in range(4) if r[3 + i].lower().startswith("active")})
+        return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": max(mx) if mx else None,
+                "reasons": reasons, "samples": len(self.rows)}
+
+
+def dist_setup():
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    if world > 1:
+        import torch.distributed as dist
+
+        dist.init_process_group("gloo")
+    return world, rank, local
+
+
+def dist_max(x, world):
+    if world == 1:
+        return x
+    import torch
+    import torch.distributed as dist
+
+    t = torch.tensor([float(x)], dtype=torch.float64)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
+def dist_barrier(world):
+    if world > 1:
+        import torch.distributed as dist
+
+        dist.barrier()
+
+
+def cpu_port_rate(conf, n, rp, col, st, steps, threads):
+    """Oracle restatement of the reference OpenMP loop on the host cores: cell-steps/s."""
+    from oracle import oracle as O
+
+    s = st.copy()
+    t0 = time.perf_counter()
+    O.run(n, conf[:23], s, rp, col, g_uniform=conf[1], nsteps=steps, trace_every=TRACE_EVERY,
+          traces=("axon",), nthreads=threads)
+    dt = time.perf_counter() - t0
+    return n * steps / dt, dt
+
+
+def run_reference(args, world, rank):
+    if rank != 0:
+        return 0
+    from oracle import oracle as O
+
+    O.build()
+    conf, n, rp, col, st = workload()
+    threads = os.cpu_count() or 1
+    sample = 100  # timesteps per bench step
+    for _ in range(args.warmup):
+        cpu_port_rate(conf, n, rp, col, st, 10, threads)
+    rates, total = [], 0.0
+    for _ in range(args.steps):
+        r, dt = cpu_port_rate(conf, n, rp, col, st, sample, threads)
+        rates.append(r)
+        total += dt
+    value = n * sample * args.steps / total
+    line = {
+        "impl": "reference", "metric": "cell-steps/s", "value": value, "unit": "cell-steps/s",
+        "n_gpus": args.gpus, "steps": args.steps, "warmup": args.warmup,
+        "ms_per_step": 1e3 * total / args.steps, "higher_is_better": True, "scaling": "weak",
+        "vs_baseline": None, "dtype": "f32", "data": "synthetic",
+        "config": {"workload": f"grid {ROWS}x{COLS} gaussian sigma={SIGMA} radius={RADIUS}, {len(col)} edges",
+                   "cells": n, "edges": int(len(col)), "timesteps_per_step": sample},
+        "cpu_baseline": {"value": value, "unit": "cell-steps/s", "cores": threads, "kind": "port",
+                         "sample": f"{sample} timesteps of the workload per bench step, OpenMP over cells"},
+        "e2e": {"value": value, "unit": "cell-steps/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+    }
+    print(json.dumps(line))
+    return 0
+
+
+def flush_l2():
+    import torch
+
+    if not hasattr(flush_l2, "buf"):
+        flush_l2.buf = torch.empty(256 << 20, dtype=torch.uint8, device="cuda")
+    flush_l2.buf.zero_()
+    torch.cuda.synchronize()
+
+
+def run_gpu(args, world, rank, local):
+    import numpy as np
+    import torch
+
+    import infoli_gb300 as ig
+    from infoli_gb300 import build
+
+    torch.cuda.set_device(local)
+    build.build()
+    conf, n, rp, col, st = workload()
+    sim = ig.Simulation(n, conf, rp, col, init_state=st, device=local)
+    plan = sim.plan_info()
+
+    rows_holder = {}
+
+    def on_row(step, what, v):
+        rows_holder["last"] = (step, v[0])
+
+    # warm-up
+    for _ in range(args.warmup):
+        sim.run_with_callback(STEPS_PER_ITER, TRACE_EVERY, ig.TRACE_AXON, on_row)
+
+    # ---- device-resident throughput (CUDA events on the simulation stream)
+    dev_ms, launches = [], 0
+    dist_barrier(world)
+    torch.cuda.synchronize()
+    t_wall0 = time.perf_counter()
+    with ClockSampler(local) as clk:
+        for _ in range(args.steps):
+            flush_l2()
+            sim.run_with_callback(STEPS_PER_ITER, TRACE_EVERY, ig.TRACE_AXON, on_row)
+            ms, nl = sim.last_run_stats()
+            dev_ms.append(ms)
+            launches += nl
+    torch.cuda.synchronize()
+    dist_barrier(world)
+    wall = time.perf_counter() - t_wall0
+    total_dev_ms = dist_max(sum(dev_ms), world)
+
+    # ---- e2e through the C ABI from host buffers
+    host_state = torch.from_numpy(st).pin_memory().numpy()
+    out_state = np.empty_like(st)
+    dist_barrier(world)
+    t0 = time.perf_counter()
+    for _ in range(args.steps):
+        sim.set_state(host_state)
+        sim.run_with_callback(STEPS_PER_ITER, TRACE_EVERY, ig.TRACE_AXON, on_row)
+        out_state[:] = sim.get_state()
+    e2e_s = dist_max(time.perf_counter() - t0, world)
+    rows_per_iter = STEPS_PER_ITER // TRACE_EVERY
+    h2d = 19 * 4 * n
+    d2h = 19 * 4 * n + rows_per_iter * 4 * n
+
+    # ---- phase profile of the kernel (separate pass, not part of the timing)
+    sim.set_profiling(True)
+    sim.run(STEPS_PER_ITER)
+    prof = sim.get_profile()
+    sim.set_profiling(False)
+    sim.close()
+
+    cell_steps = n * STEPS_PER_ITER * args.steps * world
+    value = cell_steps / (total_dev_ms * 1e-3)
+    e2e_value = cell_steps / e2e_s
+
+    # roofline of the dominant kernel (the persistent step kernel): algorithmic
+    # bytes per cell-step = 132 B of state + ceil(N/8) B of uniform-g adjacency bits
+    per_launch_steps = STEPS_PER_ITER
+    alg_bytes_per_launch = (132 + (n + 7) // 8) * n * per_launch_steps
+    launch_ms = sum(dev_ms) / max(1, launches)
+    achieved = alg_bytes_per_launch / (launch_ms * 1e-3) / 1e9
+    peak, peak_kind = peaks()
+
+    result = None
+    if rank == 0:
+        clocks = clk.summary()
+        threads = os.cpu_count() or 1
+        cpu_rate, cpu_dt = cpu_port_rate(conf, n, rp, col, st, 200, threads)
+        result = {
+            "metric": "cell-steps/s", "value": value, "unit": "cell-steps/s", "n_gpus": world,
+            "steps": args.steps, "warmup": args.warmup, "ms_per_step": total_dev_ms / args.steps,
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
+            "data": "synthetic",
+            "config": {
+                "workload": f"grid {ROWS}x{COLS} gaussian sigma={SIGMA} radius={RADIUS} g=0.04, "
+                            f"{STEPS_PER_ITER} timesteps per step, V_axon trace every {TRACE_EVERY}",
+                "cells": n, "edges": int(len(col)), "mean_degree": float(len(col) / n),
+                "timesteps_per_step": STEPS_PER_ITER, "l2": "flushed between timed steps (256 MB memset)",
+                "parallelism": f"replicas x{world}" if world > 1 else "single GPU",
+                "plan": plan,
+            },
+            "e2e": {"value": e2e_value, "unit": "cell-steps/s", "h2d_bytes_per_step": h2d,
+                    "d2h_bytes_per_step": d2h},
+            "gpu_launches": launches,
+            "wall_s": wall,
+            "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
+                         "frac": achieved / peak, "traffic": None,
+                         "note": f"algorithmic bytes (132 + N/8) per cell-step over the step kernel's mean "
+                                 f"launch time; peak {peak_kind}"},
+            "phase_ns_per_timestep": prof["max"],
+            "clocks": clocks,
+            "cpu_baseline": {"value": cpu_rate, "unit": "cell-steps/s", "cores": threads, "kind": "port",
+                             "sample": f"200 timesteps of the same workload ({cpu_dt:.1f} s)"},
+        }
+        print(json.dumps(result))
+    return 0
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=40)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
+    args = ap.parse_args()
+    world, rank, local = dist_setup()
+    if args.impl == "reference":
+        return run_reference(args, world, rank)
+    return run_gpu(args, world, rank, local)
+
+
+if __name__ == "__main__":
+    sys.exit(main())

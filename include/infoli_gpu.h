@@ -212,6 +212,19 @@ int infoli_sim_get_profile(infoli_sim* s, double mean_ns[4], double max_ns[4]);
 
 int infoli_sim_destroy(infoli_sim* s);
 
+/* Host-side check of the work planner (no GPU needed; no counterpart in the
+ * reference): plans an n-cell network for a device with grid_max co-resident
+ * CTAs of `threads` threads and smem_budget bytes of shared memory per CTA
+ * (sync_mode 0 auto, 1 grid barrier, 2 stamped words; grid 0 = automatic),
+ * then computes the gap-junction currents of the voltages vdend[n] by walking
+ * the plan's tables with the step kernel's addressing, every shared-memory
+ * offset bounds-checked.  info[8] = {CTAs, stamped, tiles, chunks or groups,
+ * partial slots, shared bytes, progress probes, resident}.  Returns 0 or a
+ * negative code naming the violated invariant. */
+int infoli_plan_emulate(int n, const int64_t* row_ptr, const int32_t* col, const float* g, float g_uniform,
+                        int grid, int grid_max, int threads, int64_t smem_budget, int sync_mode,
+                        const float* vdend, float* ic_out, int64_t info[8]);
+
 /* ------------------------------------------------------------------------ */
 /* trace text (host side)                                                    */
 /* ------------------------------------------------------------------------ */

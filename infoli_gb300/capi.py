@@ -40,7 +40,7 @@ EXPORTED = [
     "infoli_sim_set_stimulus_pulse", "infoli_sim_set_stimulus_cells", "infoli_sim_run",
     "infoli_sim_run_into", "infoli_sim_get_state", "infoli_sim_set_state", "infoli_sim_step",
     "infoli_sim_last_run_stats", "infoli_sim_plan_info", "infoli_sim_destroy", "infoli_format_f8",
-    "infoli_format_row", "infoli_sim_set_profiling", "infoli_sim_get_profile",
+    "infoli_format_row", "infoli_sim_set_profiling", "infoli_sim_get_profile", "infoli_plan_emulate",
 ]
 
 
@@ -101,6 +101,7 @@ def load():
         "infoli_sim_last_run_stats": ([P, P, P], I),
         "infoli_sim_plan_info": ([P, P, P, P, P, P], I),
         "infoli_sim_destroy": ([P], I),
+        "infoli_plan_emulate": ([I, P, P, P, F, I, I, I, I64, I, P, P, P], I),
         "infoli_sim_set_profiling": ([P, I], I),
         "infoli_sim_get_profile": ([P, P, P], I),
         "infoli_format_f8": ([C.c_char_p, F], I),
@@ -195,6 +196,24 @@ def format_row(values: np.ndarray, tagged: bool, nthreads: int = 0) -> str:
     buf = C.create_string_buffer(cap)
     k = _check(load().infoli_format_row(buf, cap, _p(v), v.size, int(bool(tagged)), nthreads))
     return buf.raw[:k].decode()
+
+
+def plan_emulate(n, row_ptr, col, vdend, g=None, g_uniform=0.04, grid=0, grid_max=152, threads=1024,
+                 smem_budget=232448 - 1024, sync_mode=0):
+    """Host walk of the planner's tables (infoli_plan_emulate): (I_c[n], info dict)."""
+    row_ptr = np.ascontiguousarray(row_ptr, dtype=np.int64)
+    col = np.ascontiguousarray(col, dtype=np.int32)
+    g = None if g is None else np.ascontiguousarray(g, dtype=np.float32)
+    v = np.ascontiguousarray(vdend, dtype=np.float32)
+    out = np.zeros(n, dtype=np.float32)
+    info = np.zeros(8, dtype=np.int64)
+    rc = load().infoli_plan_emulate(n, _p(row_ptr), _p(col) if col.size else None, _p(g), float(g_uniform),
+                                    grid, grid_max, threads, int(smem_budget), sync_mode, _p(v), _p(out),
+                                    _p(info))
+    if rc != 0:
+        raise InfoliError(rc, f"plan emulation failed with code {rc}")
+    keys = ("ctas", "stamped", "tiles", "chunks", "max_slots", "smem_bytes", "probes", "resident")
+    return out, dict(zip(keys, info.tolist()))
 
 
 def device_count() -> int:

@@ -65,6 +65,9 @@ struct infoli_sim {
   CellSlots* d_cell_slots = nullptr;
   uint16_t* d_edges = nullptr;
   float* d_edge_g = nullptr;
+  int* d_probes = nullptr;
+  int2_t* d_gdesc = nullptr;
+  unsigned long long* d_vll[2] = {nullptr, nullptr};  // stamped exchange words
   // state
   float* d_vd[2] = {nullptr, nullptr};
   float* d_st = nullptr;
@@ -101,7 +104,7 @@ void release(infoli_sim* s) {
   void* dptrs[] = {s->d_cta,   s->d_tiles,  s->d_chunks, s->d_cell_slots, s->d_edges,
                    s->d_edge_g, s->d_vd[0], s->d_vd[1],  s->d_st,         s->d_ca,
                    s->d_cell_amp, s->d_cell_onset, s->d_bar, s->d_err, s->d_trace[0], s->d_trace[1],
-                   s->d_prof};
+                   s->d_prof, s->d_probes, s->d_vll[0], s->d_vll[1], s->d_gdesc};
   for (void* p : dptrs)
     if (p) cudaFree(p);
   for (float* h : s->h_trace)
@@ -169,6 +172,11 @@ int fill_args(infoli_sim* s, StepArgs* a) {
   a->timeout_ns = wait_timeout_ns();
   a->shape = s->plan.shape;
   a->prof = s->d_prof;
+  a->vll[0] = s->d_vll[0];
+  a->vll[1] = s->d_vll[1];
+  a->probes = s->d_probes;
+  a->gdesc = reinterpret_cast<const int2*>(s->d_gdesc);
+  a->n_cells = s->n;
   return INFOLI_OK;
 }
 
@@ -189,7 +197,9 @@ int check_device_error(infoli_sim* s) {
   if (err != DEV_OK) {
     cudaMemset(s->d_err, 0, sizeof(int));
     return infoli__fail(INFOLI_ERR_TIMEOUT, "device wait gave up (code %d): %s", err,
-                        err == DEV_ERR_BARRIER_TIMEOUT ? "grid barrier timeout" : "tile copy timeout");
+                        err == DEV_ERR_BARRIER_TIMEOUT ? "grid barrier timeout"
+                        : err == DEV_ERR_STAMP_TIMEOUT ? "stamped V_dend exchange timeout"
+                                                       : "tile copy timeout");
   }
   return INFOLI_OK;
 }
@@ -256,6 +266,7 @@ int infoli_sim_create(const infoli_sim_desc* d, infoli_sim** out) {
   pin.smem_budget = (size_t)smem_optin - 1024;  // static shared (abort flag) headroom
   pin.kahan = s->kahan;
   pin.no_resident = getenv("INFOLI_NO_RESIDENT") ? 1 : 0;
+  if (const char* sm = getenv("INFOLI_SYNC")) pin.sync_mode = !strcmp(sm, "barrier") ? kSyncBarrier : !strcmp(sm, "stamped") ? kSyncStamped : kSyncAuto;
   std::string perr;
   if (!make_plan(pin, &s->plan, &perr)) return fail(infoli__fail(INFOLI_ERR_ARG, "%s", perr.c_str()));
   const int cores = max_coresident_ctas(kThreads, s->plan.smem_bytes);
@@ -268,7 +279,9 @@ int infoli_sim_create(const infoli_sim_desc* d, infoli_sim** out) {
       (rc = dev_upload(&s->d_chunks, s->plan.chunks.data(), s->plan.chunks.size())) ||
       (rc = dev_upload(&s->d_cell_slots, s->plan.cell_slots.data(), s->plan.cell_slots.size())) ||
       (rc = dev_upload(&s->d_edges, s->plan.edges.data(), s->plan.edges.size())) ||
-      (rc = dev_upload(&s->d_edge_g, s->plan.edge_g.data(), s->plan.edge_g.size())))
+      (rc = dev_upload(&s->d_edge_g, s->plan.edge_g.data(), s->plan.edge_g.size())) ||
+      (rc = dev_upload(&s->d_probes, s->plan.probes.data(), s->plan.probes.size())) ||
+      (rc = dev_upload(&s->d_gdesc, s->plan.gdesc.data(), s->plan.gdesc.size())))
     return fail(rc);
   // the kernel needs valid pointers even for empty tables
   if (!s->d_chunks && cudaMalloc((void**)&s->d_chunks, sizeof(ChunkDesc)) != cudaSuccess)
@@ -289,6 +302,11 @@ int infoli_sim_create(const infoli_sim_desc* d, infoli_sim** out) {
   cudaMemset(s->d_vd[1], 0, np * sizeof(float));
   cudaMemset(s->d_err, 0, 128);
   cudaMemset(s->d_bar, 0, 128);
+  if (s->plan.shape.stamped) {
+    if (cudaMalloc((void**)&s->d_vll[0], np * sizeof(unsigned long long)) != cudaSuccess ||
+        cudaMalloc((void**)&s->d_vll[1], np * sizeof(unsigned long long)) != cudaSuccess)
+      return fail(infoli__fail(INFOLI_ERR_NOMEM, "sim_create: device allocation failed"));
+  }
 
   std::vector<float> init;
   const float* st = d->init_state;
@@ -421,6 +439,10 @@ int infoli_sim_run(infoli_sim* s, int n_steps, int trace_every, int trace_what, 
       pend.erase(pend.begin());
     }
     CK(cudaMemsetAsync(s->d_bar, 0, sizeof(unsigned), s->stream));
+    if (s->plan.shape.stamped) {  // no stale stamp may match a step of this launch
+      CK(cudaMemsetAsync(s->d_vll[0], 0xff, (size_t)s->n_pad * sizeof(unsigned long long), s->stream));
+      CK(cudaMemsetAsync(s->d_vll[1], 0xff, (size_t)s->n_pad * sizeof(unsigned long long), s->stream));
+    }
     CK(launch_step_kernel(a, s->plan.grid, s->plan.threads, s->stream));
     ++launches;
     if (rows > 0) {

@@ -1,7 +1,7 @@
-// InfOli 3-compartment cell update on the GPU: one thread per cell, state in
-// registers.  Follows the reference's fused compartment loop
-// (src/openmp/infoli.c:556-675; struct form CompDend/CompSoma/CompAxon in
-// src/single_threaded/infoli.c:371-858) operation for operation:
+// InfOli 3-compartment cell update on the GPU.  Follows the reference's
+// fused compartment loop (src/openmp/infoli.c:556-675; struct form
+// CompDend/CompSoma/CompAxon in src/single_threaded/infoli.c:371-858)
+// operation for operation:
 //   * gates are advanced first, currents use the new gates, every voltage
 //     derivative uses the old voltages;
 //   * Ca2Plus is advanced from the old I_CaH, alpha_s uses the old Ca2Plus;
@@ -10,6 +10,12 @@
 // GPU choices: accurate expf and IEEE division as in the reference; powf with
 // an integer exponent is written as products; the Ca2+ concentration is kept
 // and advanced in FP64 (the only FP64 arithmetic on the GPU).
+//
+// The update is cut into eight independent gate units (each advances its
+// gates and returns the ionic current(s) they drive) plus one voltage step
+// that adds the currents in the reference's order.  The units only read the
+// old voltages, so they can run on different warps, and before the
+// gap-junction current of the step is known.
 #pragma once
 #include <cuda_runtime.h>
 
@@ -21,102 +27,164 @@ struct ModelParams {
       G_NA_A, G_NA_R, G_K_A, G_LA, P1, P2, G_INT, V_NA, V_K, V_CA, V_H, V_L;
 };
 
-// Evolving per-cell state (plus g_CaL, which is constant per cell).
-struct CellState {
-  float Vd, Vs, Va;       // dendrite / soma / axon voltages
-  float q, r, s;          // Hcurrent_q, Calcium_r, Potassium_s
-  double Ca;              // Ca2Plus (FP64)
-  float ICaH;             // I_CaH
-  float gCaL;             // g_CaL
-  float k, l, m, h, n, p, xs;  // Calcium_k/l, Sodium_m/h, Potassium_n/p/x_s
-  float ma, ha, xa;       // Sodium_m_a, Sodium_h_a, Potassium_x_a
+struct Volts {
+  float Vd, Vs, Va;  // dendrite / soma / axon
 };
+
+// Gate state of one cell (plus g_CaL, constant per cell).
+struct Gates {
+  float q, r, s;               // Hcurrent_q, Calcium_r, Potassium_s
+  double Ca;                   // Ca2Plus (FP64)
+  float ICaH;                  // I_CaH (previous step's high-threshold Ca current)
+  float gCaL;                  // g_CaL
+  float k, l, m, h, n, p, xs;  // Calcium_k/l, Sodium_m/h, Potassium_n/p/x_s
+  float ma, ha, xa;            // Sodium_m_a, Sodium_h_a, Potassium_x_a
+};
+
+// Ionic currents produced by the gate units.
+struct Currents {
+  float I_h, I_CaH, I_K_Ca;               // dendrite
+  float I_CaL, I_Na_s, I_Kdr_s, I_K_s;    // soma
+  float I_Na_a, I_K_a;                    // axon
+};
+
+enum { kUnits = 8 };
 
 __device__ __forceinline__ float sq(float x) { return x * x; }
 
-// One explicit-Euler step of one cell.  I_c: gap-junction current into the
-// dendrite; iApp: applied dendritic current.
-__device__ __forceinline__ void cell_step(const ModelParams& P, CellState& c, float I_c, float iApp) {
-  const float Vd = c.Vd, Vs = c.Vs, Va = c.Va;
-
-  // ---- dendrite (src/openmp/infoli.c:560-593)
+// ---- dendrite (src/openmp/infoli.c:560-593)
+// unit 0: H current gate q
+__device__ __forceinline__ void unit_q(const ModelParams& P, const Volts& v, Gates& g, Currents& c) {
+  const float Vd = v.Vd;
   const float q_inf = 1.0f / (1.0f + expf((Vd + 80.0f) / 4.0f));
   const float tau_q = 1.0f / (expf(-0.086f * Vd - 14.6f) + expf(0.070f * Vd - 1.87f));
-  c.q = P.DELTA * ((q_inf - c.q) / tau_q) + c.q;
+  g.q = P.DELTA * ((q_inf - g.q) / tau_q) + g.q;
+  c.I_h = P.G_H * g.q * (Vd - P.V_H);
+}
+// unit 1: high-threshold Ca gate r, Ca-dependent K gate s, Ca2+ concentration
+__device__ __forceinline__ void unit_rs(const ModelParams& P, const Volts& v, Gates& g, Currents& c) {
+  const float Vd = v.Vd;
   const float alpha_r = 1.7f / (1.0f + expf(-(Vd - 5.0f) / 13.9f));
   const float beta_r = 0.02f * (Vd + 8.5f) / (expf((Vd + 8.5f) / 5.0f) - 1.0f);
   const float r_inf = alpha_r / (alpha_r + beta_r);
   const float tau_r = 5.0f / (alpha_r + beta_r);
-  c.r = P.DELTA * ((r_inf - c.r) / tau_r) + c.r;
-  const float ca_f = (float)c.Ca;
-  const float alpha_s = fminf(0.00002f * ca_f, 0.01f);
+  g.r = P.DELTA * ((r_inf - g.r) / tau_r) + g.r;
+  const float alpha_s = fminf(0.00002f * (float)g.Ca, 0.01f);
   const float beta_s = 0.015f;
   const float s_inf = alpha_s / (alpha_s + beta_s);
   const float tau_s = 1.0f / (alpha_s + beta_s);
-  c.s = P.DELTA * ((s_inf - c.s) / tau_s) + c.s;
-  {  // FP64 Ca2+ concentration, old I_CaH and old Ca2Plus (:583-584)
-    const double dCa_dt = -3.0 * (double)c.ICaH - 0.075 * c.Ca;
-    c.Ca = (double)P.DELTA * dCa_dt + c.Ca;
+  g.s = P.DELTA * ((s_inf - g.s) / tau_s) + g.s;
+  {  // FP64 Ca2+ concentration from the old I_CaH and old Ca2Plus (:583-584)
+    const double dCa_dt = -3.0 * (double)g.ICaH - 0.075 * g.Ca;
+    g.Ca = (double)P.DELTA * dCa_dt + g.Ca;
   }
-  const float I_sd = (P.G_INT / (1.0f - P.P1)) * (Vd - Vs);
-  const float I_CaH = P.G_CAH * sq(c.r) * (Vd - P.V_CA);
-  const float I_K_Ca = P.G_K_CA * c.s * (Vd - P.V_K);
-  const float I_ld = P.G_LD * (Vd - P.V_L);
-  const float I_h = P.G_H * c.q * (Vd - P.V_H);
-  const float dVd_dt = (-(I_CaH + I_sd + I_ld + I_K_Ca + I_c + I_h) + iApp) / P.C_M;
-  c.ICaH = I_CaH;
+  c.I_CaH = P.G_CAH * sq(g.r) * (Vd - P.V_CA);
+  c.I_K_Ca = P.G_K_CA * g.s * (Vd - P.V_K);
+  g.ICaH = c.I_CaH;
+}
 
-  // ---- soma (:598-642)
+// ---- soma (:598-642)
+// unit 2: low-threshold Ca gates k, l
+__device__ __forceinline__ void unit_kl(const ModelParams& P, const Volts& v, Gates& g, Currents& c) {
+  const float Vs = v.Vs;
   const float k_inf = 1.0f / (1.0f + expf(-(Vs + 61.0f) / 4.2f));
   const float l_inf = 1.0f / (1.0f + expf((Vs + 85.5f) / 8.5f));
   const float tau_l = (20.0f * expf((Vs + 160.0f) / 30.0f) / (1.0f + expf((Vs + 84.0f) / 7.3f))) + 35.0f;
-  c.k = P.DELTA * (k_inf - c.k) + c.k;  // tau_k = 1
-  c.l = P.DELTA * ((l_inf - c.l) / tau_l) + c.l;
+  g.k = P.DELTA * (k_inf - g.k) + g.k;  // tau_k = 1
+  g.l = P.DELTA * ((l_inf - g.l) / tau_l) + g.l;
+  c.I_CaL = g.gCaL * (g.k * g.k * g.k) * g.l * (Vs - P.V_CA);
+}
+// unit 3: Na gates m (instantaneous), h
+__device__ __forceinline__ void unit_mh(const ModelParams& P, const Volts& v, Gates& g, Currents& c) {
+  const float Vs = v.Vs;
   const float m_inf = 1.0f / (1.0f + expf((-30.0f - Vs) / 5.5f));
   const float h_inf = 1.0f / (1.0f + expf((-70.0f - Vs) / -5.8f));
   const float tau_h = 3.0f * expf((-40.0f - Vs) / 33.0f);
-  c.m = m_inf;
-  c.h = c.h + P.DELTA * ((h_inf - c.h) / tau_h);
+  g.m = m_inf;
+  g.h = g.h + P.DELTA * ((h_inf - g.h) / tau_h);
+  c.I_Na_s = P.G_NA_S * (g.m * g.m * g.m) * g.h * (Vs - P.V_NA);
+}
+// unit 4: delayed-rectifier K gates n, p (p is advanced but drives no current)
+__device__ __forceinline__ void unit_np(const ModelParams& P, const Volts& v, Gates& g, Currents& c) {
+  const float Vs = v.Vs;
   const float n_inf = 1.0f / (1.0f + expf((-3.0f - Vs) / 10.0f));
   const float p_inf = 1.0f / (1.0f + expf((-51.0f - Vs) / -12.0f));
   const float tau_n = 5.0f + (47.0f * expf(-(-50.0f - Vs) / 900.0f));
-  c.n = P.DELTA * ((n_inf - c.n) / tau_n) + c.n;
-  c.p = P.DELTA * ((p_inf - c.p) / tau_n) + c.p;
+  g.n = P.DELTA * ((n_inf - g.n) / tau_n) + g.n;
+  g.p = P.DELTA * ((p_inf - g.p) / tau_n) + g.p;
+  c.I_Kdr_s = P.G_KDR_S * sq(sq(g.n)) * (Vs - P.V_K);
+}
+// unit 5: voltage-dependent K gate x_s (literal 0.05 step, :632)
+__device__ __forceinline__ void unit_xs(const ModelParams& P, const Volts& v, Gates& g, Currents& c) {
+  const float Vs = v.Vs;
   const float alpha_x_s = 0.13f * (Vs + 25.0f) / (1.0f - expf(-(Vs + 25.0f) / 10.0f));
   const float beta_x_s = 1.69f * expf(-0.0125f * (Vs + 35.0f));
   const float x_inf_s = alpha_x_s / (alpha_x_s + beta_x_s);
   const float tau_x_s = 1.0f / (alpha_x_s + beta_x_s);
-  c.xs = 0.05f * ((x_inf_s - c.xs) / tau_x_s) + c.xs;
-  const float I_ds = (P.G_INT / P.P1) * (Vs - Vd);
-  const float I_CaL = c.gCaL * (c.k * c.k * c.k) * c.l * (Vs - P.V_CA);
-  const float I_Na_s = P.G_NA_S * (c.m * c.m * c.m) * c.h * (Vs - P.V_NA);
-  const float I_ls = P.G_LS * (Vs - P.V_L);
-  const float I_Kdr_s = P.G_KDR_S * sq(sq(c.n)) * (Vs - P.V_K);
-  const float I_K_s = P.G_K_S * sq(sq(c.xs)) * (Vs - P.V_K);
-  const float I_as = (P.G_INT / (1.0f - P.P2)) * (Vs - Va);
-  const float dVs_dt = (-(I_CaL + I_ds + I_as + I_Na_s + I_ls + I_Kdr_s + I_K_s)) / P.C_M;
+  g.xs = 0.05f * ((x_inf_s - g.xs) / tau_x_s) + g.xs;
+  c.I_K_s = P.G_K_S * sq(sq(g.xs)) * (Vs - P.V_K);
+}
 
-  // ---- axon (:647-668)
+// ---- axon (:647-668)
+// unit 6: Na gates m_a (instantaneous), h_a
+__device__ __forceinline__ void unit_mha(const ModelParams& P, const Volts& v, Gates& g, Currents& c) {
+  const float Va = v.Va;
   const float m_inf_a = 1.0f / (1.0f + expf((-30.0f - Va) / 5.5f));
   const float h_inf_a = 1.0f / (1.0f + expf((-60.0f - Va) / -5.8f));
   const float tau_h_a = 1.5f * expf((-40.0f - Va) / 33.0f);
-  c.ma = m_inf_a;
-  c.ha = c.ha + P.DELTA * ((h_inf_a - c.ha) / tau_h_a);
+  g.ma = m_inf_a;
+  g.ha = g.ha + P.DELTA * ((h_inf_a - g.ha) / tau_h_a);
+  c.I_Na_a = P.G_NA_A * (g.ma * g.ma * g.ma) * g.ha * (Va - P.V_NA);
+}
+// unit 7: K gate x_a (literal 0.05 step, :661)
+__device__ __forceinline__ void unit_xa(const ModelParams& P, const Volts& v, Gates& g, Currents& c) {
+  const float Va = v.Va;
   const float alpha_x_a = 0.13f * (Va + 25.0f) / (1.0f - expf(-(Va + 25.0f) / 10.0f));
   const float beta_x_a = 1.69f * expf(-0.0125f * (Va + 35.0f));
   const float x_inf_a = alpha_x_a / (alpha_x_a + beta_x_a);
   const float tau_x_a = 1.0f / (alpha_x_a + beta_x_a);
-  c.xa = 0.05f * ((x_inf_a - c.xa) / tau_x_a) + c.xa;
-  const float I_Na_a = P.G_NA_A * (c.ma * c.ma * c.ma) * c.ha * (Va - P.V_NA);
+  g.xa = 0.05f * ((x_inf_a - g.xa) / tau_x_a) + g.xa;
+  c.I_K_a = P.G_K_A * sq(sq(g.xa)) * (Va - P.V_K);
+}
+
+// Run the units whose bit is set in `mask` (bit u = unit u).
+__device__ __forceinline__ void run_units(const ModelParams& P, unsigned mask, const Volts& v, Gates& g,
+                                          Currents& c) {
+  if (mask & 0x01u) unit_q(P, v, g, c);
+  if (mask & 0x02u) unit_rs(P, v, g, c);
+  if (mask & 0x04u) unit_kl(P, v, g, c);
+  if (mask & 0x08u) unit_mh(P, v, g, c);
+  if (mask & 0x10u) unit_np(P, v, g, c);
+  if (mask & 0x20u) unit_xs(P, v, g, c);
+  if (mask & 0x40u) unit_mha(P, v, g, c);
+  if (mask & 0x80u) unit_xa(P, v, g, c);
+}
+
+// Voltage step (:587-592, :635-642, :664-675): currents summed in the
+// reference's order, all from the old voltages.  I_c: gap-junction current.
+__device__ __forceinline__ void voltage_step(const ModelParams& P, Volts& v, const Currents& c, float I_c,
+                                             float iApp) {
+  const float Vd = v.Vd, Vs = v.Vs, Va = v.Va;
+  const float I_sd = (P.G_INT / (1.0f - P.P1)) * (Vd - Vs);
+  const float I_ld = P.G_LD * (Vd - P.V_L);
+  const float dVd_dt = (-(c.I_CaH + I_sd + I_ld + c.I_K_Ca + I_c + c.I_h) + iApp) / P.C_M;
+  const float I_ds = (P.G_INT / P.P1) * (Vs - Vd);
+  const float I_ls = P.G_LS * (Vs - P.V_L);
+  const float I_as = (P.G_INT / (1.0f - P.P2)) * (Vs - Va);
+  const float dVs_dt = (-(c.I_CaL + I_ds + I_as + c.I_Na_s + I_ls + c.I_Kdr_s + c.I_K_s)) / P.C_M;
   const float I_la = P.G_LA * (Va - P.V_L);
   const float I_sa = (P.G_INT / P.P2) * (Va - Vs);
-  const float I_K_a = P.G_K_A * sq(sq(c.xa)) * (Va - P.V_K);
-  const float dVa_dt = (-(I_K_a + I_sa + I_la + I_Na_a)) / P.C_M;
+  const float dVa_dt = (-(c.I_K_a + I_sa + I_la + c.I_Na_a)) / P.C_M;
+  v.Vd = P.DELTA * dVd_dt + Vd;
+  v.Vs = P.DELTA * dVs_dt + Vs;
+  v.Va = P.DELTA * dVa_dt + Va;
+}
 
-  // ---- new voltages (:673-675)
-  c.Vd = P.DELTA * dVd_dt + Vd;
-  c.Vs = P.DELTA * dVs_dt + Vs;
-  c.Va = P.DELTA * dVa_dt + Va;
+// The whole step of one cell on one thread.
+__device__ __forceinline__ void cell_step(const ModelParams& P, Volts& v, Gates& g, float I_c, float iApp) {
+  Currents c;
+  run_units(P, 0xffu, v, g, c);
+  voltage_step(P, v, c, I_c, iApp);
 }
 
 }  // namespace infoli

@@ -76,14 +76,179 @@ __device__ __forceinline__ bool grid_sync(const StepArgs& a, unsigned target, vo
   return *s_abort == 0;
 }
 
+
+__device__ __forceinline__ unsigned long long pack_stamp(float v, unsigned stamp) {
+  return ((unsigned long long)stamp << 32) | (unsigned long long)__float_as_uint(v);
+}
+
+// Stamped exchange: copy words of slot `src` into dst (if not null) once their
+// stamp equals `want`.  Word i is src[lo + i], or src[list[i]] when list is
+// given.  Words of cells >= n_cells are never published and read as 0.
+// Each thread keeps up to four loads in flight; the wait is bounded by the
+// launch's timeout (error recorded, false returned).
+__device__ __forceinline__ bool poll_words(const StepArgs& a, const unsigned long long* src, int lo, int count,
+                                        const int* list, float* dst, unsigned want) {
+  const int T = blockDim.x;
+  uint64_t t0 = 0;
+  for (int base = threadIdx.x; base < count; base += 4 * T) {
+    unsigned long long w[4];
+    int cellid[4];
+    unsigned pend = 0;
+#pragma unroll
+    for (int k = 0; k < 4; ++k) {
+      const int i = base + k * T;
+      cellid[k] = -1;
+      if (i < count) {
+        const int c = list ? list[i] : lo + i;
+        if (c < a.n_cells) {
+          cellid[k] = c;
+          w[k] = ld_relaxed_gpu_u64(src + c);
+          pend |= 1u << k;
+        } else if (dst) {
+          dst[i] = 0.0f;
+        }
+      }
+    }
+    while (true) {
+#pragma unroll
+      for (int k = 0; k < 4; ++k) {
+        if (((pend >> k) & 1u) && (unsigned)(w[k] >> 32) == want) {
+          if (dst) dst[base + k * T] = __uint_as_float((unsigned)w[k]);
+          pend &= ~(1u << k);
+        }
+      }
+      if (!pend) break;
+      const uint64_t now = globaltimer_ns();
+      if (t0 == 0) {
+        t0 = now;
+      } else if (now - t0 > a.timeout_ns || ld_relaxed_gpu(a.err) != 0) {
+        atomicCAS(a.err, 0, DEV_ERR_STAMP_TIMEOUT);
+        return false;
+      }
+#pragma unroll
+      for (int k = 0; k < 4; ++k)
+        if ((pend >> k) & 1u) w[k] = ld_relaxed_gpu_u64(src + cellid[k]);
+    }
+  }
+  return true;
+}
+
+// Phase A of stamped plans (packed lane-chunk layout, all in shared memory):
+// warp w takes groups w, w + nwarps, ... < ngroups; lane l of the warp owns
+// lane-chunk l of the group (up to kLaneEdges edges of one receiver) and
+// reduces it alone -- no cross-lane reduction.  Each 8-byte load brings the
+// lane's next four byte offsets; padding entries address the receiver's own
+// V_dend and add exactly 0.  Two accumulators (even / odd entries) shorten
+// the dependent add chain; they are combined in a fixed order.
 template <bool KAHAN, bool EDGE_G>
+__device__ __forceinline__ void couple_packed(const unsigned char* sm, const SmemLayout& L, int ngroups,
+                                              const float* sVd, float* part, float* partc, int warp, int nwarps,
+                                              int lane) {
+  const int2* gd = reinterpret_cast<const int2*>(sm + L.chunks);
+  const uint2* ent = reinterpret_cast<const uint2*>(sm + L.edges);
+  const float4* gv = reinterpret_cast<const float4*>(sm + L.eg);
+  for (int gi = warp; gi < ngroups; gi += nwarps) {
+    const int2 d = gd[gi * 32 + lane];  // {slot, recv}
+    const float vc = sVd[d.y];
+    float acc0 = 0.0f, acc1 = 0.0f, cmp0 = 0.0f, cmp1 = 0.0f;
+#pragma unroll 2
+    for (int kq = 0; kq < kQuads; ++kq) {
+      const int qi = (gi * kQuads + kq) * 32 + lane;
+      const uint2 o = ent[qi];
+      float4 g4 = make_float4(1.0f, 1.0f, 1.0f, 1.0f);
+      if (EDGE_G) g4 = gv[qi];
+      const unsigned off[4] = {o.x & 0xffffu, o.x >> 16, o.y & 0xffffu, o.y >> 16};
+      const float gg[4] = {g4.x, g4.y, g4.z, g4.w};
+#pragma unroll
+      for (int j = 0; j < 4; ++j) {
+        const float V = vc - *reinterpret_cast<const float*>(sm + off[j]);
+        const float f = fmaf(0.8f, ex2_approx((V * V) * kNegLog2eOver100), 0.2f);
+        const float term = EDGE_G ? (gg[j] * f) * V : f * V;
+        float& acc = (j & 1) ? acc1 : acc0;
+        float& cmp = (j & 1) ? cmp1 : cmp0;
+        if (KAHAN) {
+          const float y = term - cmp;
+          const float s = acc + y;
+          cmp = (s - acc) - y;
+          acc = s;
+        } else {
+          acc += term;
+        }
+      }
+    }
+    part[d.x] = acc0 + acc1;
+    if (KAHAN) partc[d.x] = cmp0 + cmp1;
+  }
+}
+
+// Phase A for one staged tile: warp w reduces chunks cb+w, cb+w+nwarps, ...
+// Each lane takes edges lane, lane+32, ... of the chunk (predicated, fully
+// unrolled); a shuffle tree sums the lanes; lane 0 writes the chunk's slot.
+template <bool KAHAN, bool EDGE_G>
+__device__ __forceinline__ void couple_tile(const ChunkDesc* chunks, const uint16_t* edges, const float* edge_g,
+                                            int cb, int ce, int edge0, const float* buf, const float* sVd,
+                                            float* part, float* partc, int warp, int nwarps, int lane) {
+  for (int ci = cb + warp; ci < ce; ci += nwarps) {
+    const ChunkDesc c = chunks[ci];
+    const float vc = sVd[c.recv];
+    const int eb = c.edge_begin - edge0;
+    float acc = 0.0f, comp = 0.0f;
+#pragma unroll
+    for (int q = 0; q < kChunkEdges / 32; ++q) {
+      const int u = lane + 32 * q;
+      if (u < c.count) {
+        const int e = eb + u;
+        const float V = vc - buf[edges[e]];
+        const float f = fmaf(0.8f, ex2_approx((V * V) * kNegLog2eOver100), 0.2f);
+        float term;
+        if (EDGE_G)
+          term = (edge_g[e] * f) * V;
+        else
+          term = f * V;
+        if (KAHAN) {
+          const float y = term - comp;
+          const float s = acc + y;
+          comp = (s - acc) - y;
+          acc = s;
+        } else {
+          acc += term;
+        }
+      }
+    }
+    if (KAHAN) {
+      // carry the compensation separately through the tree
+#pragma unroll
+      for (int o = 16; o > 0; o >>= 1) {
+        acc += __shfl_xor_sync(0xffffffffu, acc, o);
+        comp += __shfl_xor_sync(0xffffffffu, comp, o);
+      }
+      if (lane == 0) {
+        part[c.slot] = acc;
+        partc[c.slot] = comp;
+      }
+    } else {
+#pragma unroll
+      for (int o = 16; o > 0; o >>= 1) acc += __shfl_xor_sync(0xffffffffu, acc, o);
+      if (lane == 0) part[c.slot] = acc;
+    }
+  }
+}
+
+template <bool KAHAN, bool EDGE_G, bool LL>
 __global__ void __launch_bounds__(1024, 1) step_kernel(const __grid_constant__ StepArgs a) {
   extern __shared__ __align__(16) unsigned char smem_raw[];
   __shared__ int s_abort;
+  __shared__ unsigned long long s_prof[5];
   const SmemShape shp = a.shape;
   const SmemLayout L = smem_layout(shp);
   float* tbuf = reinterpret_cast<float*>(smem_raw + L.tiles);
-  float* vown = reinterpret_cast<float*>(smem_raw + L.vown);
+  // per-cell arrays: V_dend, V_soma, V_axon, then the nine unit currents
+  float* sV = reinterpret_cast<float*>(smem_raw + L.vown);
+  const int cap = shp.cells_cap;
+  float* sVd = sV;
+  float* sVs = sV + cap;
+  float* sVa = sV + 2 * cap;
+  float* sI = sV + 3 * cap;  // current k of cell r at sI[k * cap + r]
   float* part = reinterpret_cast<float*>(smem_raw + L.part);
   float* partc = reinterpret_cast<float*>(smem_raw + L.partc);
   uint64_t* mbar = reinterpret_cast<uint64_t*>(smem_raw + L.mbar);
@@ -93,11 +258,23 @@ __global__ void __launch_bounds__(1024, 1) step_kernel(const __grid_constant__ S
   const int lane = tid & 31;
   const int warp = tid >> 5;
   const int nwarps = blockDim.x >> 5;
-  const bool owner = tid < w.n_cells;
+  const bool owner = tid < w.n_cells;  // voltage thread of cell w.cell_begin + tid
   const int cell = w.cell_begin + tid;
   const long long np = a.n_pad;
   const int tile_cap = shp.tile_cap;
   const int nbuf = shp.nbuf;
+
+  // ---- gate units: warp w works on cell group w / U (32 cells) and runs
+  // the units u with u % U == w % U; U is the largest of 8, 4, 2, 1 whose
+  // groups x U fit in the CTA's warps.  Warp-uniform, so no divergence.
+  const int ngroups = (w.n_cells + 31) >> 5;
+  int U = kUnits;
+  while (U > 1 && ngroups * U > nwarps) U >>= 1;
+  const bool unit_warp = warp < ngroups * U;
+  const int ucell_l = (warp / U) * 32 + lane;  // local cell of this unit lane
+  const bool unit_lane = unit_warp && ucell_l < w.n_cells;
+  unsigned umask = 0;
+  for (int u = warp % U; u < kUnits; u += U) umask |= 1u << u;
 
   // ---- static work: either resident in shared memory or read from global.
   // Indices below are relative to the CTA's first chunk / edge.
@@ -106,12 +283,28 @@ __global__ void __launch_bounds__(1024, 1) step_kernel(const __grid_constant__ S
   const uint16_t* edges = a.edges;
   const float* edge_g = a.edge_g;
   int chunk0 = 0, edge0 = 0;
-  if (w.n_tiles > 0) {
+  if (LL) {
+    // stamped plans: tiles + packed lane-chunk groups, copied once per launch
+    TileDesc* s_t = reinterpret_cast<TileDesc*>(smem_raw + L.tdesc);
+    int2* s_d = reinterpret_cast<int2*>(smem_raw + L.chunks);
+    uint2* s_e = reinterpret_cast<uint2*>(smem_raw + L.edges);
+    float4* s_g = reinterpret_cast<float4*>(smem_raw + L.eg);
+    for (int i = tid; i < w.n_tiles; i += blockDim.x) s_t[i] = tiles[i];
+    const int nd = w.n_groups * 32;
+    for (int i = tid; i < nd; i += blockDim.x) s_d[i] = a.gdesc[(size_t)w.group_begin * 32 + i];
+    const int nq = w.n_groups * (kGroupEntries / 4);  // 8-byte quads
+    const uint2* ge = reinterpret_cast<const uint2*>(a.edges) + (size_t)w.group_begin * (kGroupEntries / 4);
+    for (int i = tid; i < nq; i += blockDim.x) s_e[i] = ge[i];
+    if (EDGE_G) {
+      const float4* gg = reinterpret_cast<const float4*>(a.edge_g) + (size_t)w.group_begin * (kGroupEntries / 4);
+      for (int i = tid; i < nq; i += blockDim.x) s_g[i] = gg[i];
+    }
+    tiles = s_t;
+  } else if (w.n_tiles > 0) {
     chunk0 = tiles[0].chunk_begin;
     const int chunk1 = tiles[w.n_tiles - 1].chunk_end;
     edge0 = chunk1 > chunk0 ? a.chunks[chunk0].edge_begin : 0;
-    const bool resident = shp.res_chunks > 0;
-    if (resident) {
+    if (shp.res_chunks > 0) {
       TileDesc* s_t = reinterpret_cast<TileDesc*>(smem_raw + L.tdesc);
       ChunkDesc* s_c = reinterpret_cast<ChunkDesc*>(smem_raw + L.chunks);
       uint16_t* s_e = reinterpret_cast<uint16_t*>(smem_raw + L.edges);
@@ -153,32 +346,37 @@ __global__ void __launch_bounds__(1024, 1) step_kernel(const __grid_constant__ S
     s_abort = 0;
   }
 
-  CellState cs;
+  // unit lanes hold the gate state of their cell in registers
+  Gates gs;
+  if (unit_lane) {
+    const int c = w.cell_begin + ucell_l;
+    const float* st = a.st;
+    gs.q = st[F_Q * np + c];
+    gs.r = st[F_R * np + c];
+    gs.s = st[F_S * np + c];
+    gs.Ca = a.ca[c];
+    gs.ICaH = st[F_ICAH * np + c];
+    gs.gCaL = st[F_GCAL * np + c];
+    gs.k = st[F_K * np + c];
+    gs.l = st[F_L * np + c];
+    gs.m = st[F_M * np + c];
+    gs.h = st[F_H * np + c];
+    gs.n = st[F_N * np + c];
+    gs.p = st[F_P * np + c];
+    gs.xs = st[F_XS * np + c];
+    gs.ma = st[F_MA * np + c];
+    gs.ha = st[F_HA * np + c];
+    gs.xa = st[F_XA * np + c];
+  }
+  // voltage threads hold the per-cell constants of the voltage step
   int2 slots = make_int2(0, 0);
   float gscale = a.g_uniform;
   float my_amp = 0.0f;
   int my_onset = 0, my_off = 0;
   if (owner) {
-    const float* st = a.st;
-    cs.Vd = a.vd[a.step0 & 1][cell];
-    cs.Vs = st[F_VS * np + cell];
-    cs.Va = st[F_VA * np + cell];
-    cs.q = st[F_Q * np + cell];
-    cs.r = st[F_R * np + cell];
-    cs.s = st[F_S * np + cell];
-    cs.Ca = a.ca[cell];
-    cs.ICaH = st[F_ICAH * np + cell];
-    cs.gCaL = st[F_GCAL * np + cell];
-    cs.k = st[F_K * np + cell];
-    cs.l = st[F_L * np + cell];
-    cs.m = st[F_M * np + cell];
-    cs.h = st[F_H * np + cell];
-    cs.n = st[F_N * np + cell];
-    cs.p = st[F_P * np + cell];
-    cs.xs = st[F_XS * np + cell];
-    cs.ma = st[F_MA * np + cell];
-    cs.ha = st[F_HA * np + cell];
-    cs.xa = st[F_XA * np + cell];
+    sVd[tid] = a.vd[a.step0 & 1][cell];
+    sVs[tid] = a.st[F_VS * np + cell];
+    sVa[tid] = a.st[F_VA * np + cell];
     slots = a.cell_slots[cell];
     if (a.cell_g) gscale = a.cell_g[cell];
     if (a.stim_kind == STIM_CELL) {
@@ -186,30 +384,72 @@ __global__ void __launch_bounds__(1024, 1) step_kernel(const __grid_constant__ S
       my_onset = a.cell_onset[cell];
     }
     if (a.cell_step_off) my_off = a.cell_step_off[cell];
-    vown[tid] = cs.Vd;
   }
+  const bool prof = a.prof != nullptr && tid == 0;
+  if (prof) s_prof[0] = s_prof[1] = s_prof[2] = s_prof[3] = s_prof[4] = 0;
   __syncthreads();
 
-  const bool prof = a.prof != nullptr && tid == 0;
-  __shared__ unsigned long long s_prof[5];
-  if (prof) s_prof[0] = s_prof[1] = s_prof[2] = s_prof[3] = s_prof[4] = 0;
   uint64_t t_step = prof ? globaltimer_ns() : 0;
-
   unsigned nload = 0;  // bulk tile loads issued so far (same value in every thread)
   int row = 0;
   unsigned bar_target = 0;
+  if (LL && owner) {
+    // publish V^step0 with its stamp (the host cleared both slots before launch)
+    st_relaxed_gpu_u64(a.vll[a.step0 & 1] + cell, pack_stamp(sVd[tid], (unsigned)a.step0));
+  }
   for (int t = 0; t < a.n_steps; ++t) {
     const int step = a.step0 + t;
     const float* vcur = a.vd[step & 1];
     uint64_t t_ready = 0;
 
-    // ---------------- stage tiles + phase A (coupling)
-    if (w.n_tiles > 0) {
-      if (tid == 0) {
-        fence_proxy_async_global();
-        fence_proxy_async_smem();
-        issue_tile(a, vcur, tiles[0], tbuf + (nload % nbuf) * tile_cap, &mbar[nload % nbuf]);
+    // ---------------- first tile in flight while the gate units run
+    if (!LL && w.n_tiles > 0 && tid == 0) {
+      fence_proxy_async_global();
+      fence_proxy_async_smem();
+      issue_tile(a, vcur, tiles[0], tbuf + (nload % nbuf) * tile_cap, &mbar[nload % nbuf]);
+    }
+
+    // ---------------- gate units (old voltages only)
+    if (unit_lane) {
+      Volts v;
+      v.Vd = sVd[ucell_l];
+      v.Vs = sVs[ucell_l];
+      v.Va = sVa[ucell_l];
+      Currents cur;
+      run_units(a.P, umask, v, gs, cur);
+      if (umask & 0x01u) sI[0 * cap + ucell_l] = cur.I_h;
+      if (umask & 0x02u) {
+        sI[1 * cap + ucell_l] = cur.I_CaH;
+        sI[2 * cap + ucell_l] = cur.I_K_Ca;
       }
+      if (umask & 0x04u) sI[3 * cap + ucell_l] = cur.I_CaL;
+      if (umask & 0x08u) sI[4 * cap + ucell_l] = cur.I_Na_s;
+      if (umask & 0x10u) sI[5 * cap + ucell_l] = cur.I_Kdr_s;
+      if (umask & 0x20u) sI[6 * cap + ucell_l] = cur.I_K_s;
+      if (umask & 0x40u) sI[7 * cap + ucell_l] = cur.I_Na_a;
+      if (umask & 0x80u) sI[8 * cap + ucell_l] = cur.I_K_a;
+    }
+
+    // ---------------- phase A: gap-junction coupling
+    if (LL) {
+      // stamped exchange: gather every tile (and the progress probes) once
+      // the words carry this step's stamp, then reduce all chunks
+      const unsigned long long* src = a.vll[step & 1];
+      int toff = 0;
+      bool ok = true;
+      for (int j = 0; j < w.n_tiles && ok; ++j) {
+        const TileDesc td = tiles[j];
+        ok = poll_words(a, src, td.lo, td.nfloats, nullptr, tbuf + toff, (unsigned)step);
+        toff += td.nfloats;
+      }
+      if (ok && w.n_probes > 0) ok = poll_words(a, src, 0, w.n_probes, a.probes + w.probe_begin, nullptr, (unsigned)step);
+      if (!ok) s_abort = 1;
+      __syncthreads();
+      if (s_abort) break;
+      if (prof) t_ready = globaltimer_ns();
+      couple_packed<KAHAN, EDGE_G>(smem_raw, L, w.n_groups, sVd, part, partc, warp, nwarps, lane);
+      __syncthreads();
+    } else if (w.n_tiles > 0) {
       for (int j = 0; j < w.n_tiles; ++j) {
         const TileDesc td = tiles[j];
         const unsigned k = nload + j;
@@ -226,57 +466,18 @@ __global__ void __launch_bounds__(1024, 1) step_kernel(const __grid_constant__ S
         }
         if (!wait_tile(a, &mbar[b], (k / (unsigned)nbuf) & 1u)) s_abort = 1;
         if (prof && j == 0) t_ready = globaltimer_ns();
-
-        for (int ci = td.chunk_begin - chunk0 + warp; ci < td.chunk_end - chunk0; ci += nwarps) {
-          const ChunkDesc c = chunks[ci];
-          const float vc = vown[c.recv];
-          const int eb = c.edge_begin - edge0;
-          float acc = 0.0f, comp = 0.0f;
-#pragma unroll 4
-          for (int u = lane; u < c.count; u += 32) {
-            const int e = eb + u;
-            const float V = vc - buf[edges[e]];
-            const float f = fmaf(0.8f, ex2_approx((V * V) * kNegLog2eOver100), 0.2f);
-            float term;
-            if (EDGE_G)
-              term = (edge_g[e] * f) * V;
-            else
-              term = f * V;
-            if (KAHAN) {
-              const float y = term - comp;
-              const float s = acc + y;
-              comp = (s - acc) - y;
-              acc = s;
-            } else {
-              acc += term;
-            }
-          }
-          if (KAHAN) {
-            // carry the compensation separately through the tree
-#pragma unroll
-            for (int o = 16; o > 0; o >>= 1) {
-              acc += __shfl_xor_sync(0xffffffffu, acc, o);
-              comp += __shfl_xor_sync(0xffffffffu, comp, o);
-            }
-            if (lane == 0) {
-              part[c.slot] = acc;
-              partc[c.slot] = comp;
-            }
-          } else {
-#pragma unroll
-            for (int o = 16; o > 0; o >>= 1) acc += __shfl_xor_sync(0xffffffffu, acc, o);
-            if (lane == 0) part[c.slot] = acc;
-          }
-        }
+        couple_tile<KAHAN, EDGE_G>(chunks, edges, edge_g, td.chunk_begin - chunk0, td.chunk_end - chunk0, edge0,
+                                   buf, sVd, part, partc, warp, nwarps, lane);
         __syncthreads();
       }
       nload += w.n_tiles;
-    } else if (prof) {
-      t_ready = globaltimer_ns();
+    } else {
+      if (prof) t_ready = globaltimer_ns();
+      __syncthreads();
     }
-    uint64_t t_coupled = prof ? globaltimer_ns() : 0;
+    const uint64_t t_coupled = prof ? globaltimer_ns() : 0;
 
-    // ---------------- phase B (fused compartment update)
+    // ---------------- phase B: voltage step, one thread per owned cell
     if (owner) {
       float ic;
       if (KAHAN) {
@@ -301,20 +502,51 @@ __global__ void __launch_bounds__(1024, 1) step_kernel(const __grid_constant__ S
         iapp = (ls >= my_onset && ls < my_onset + a.stim_dur) ? my_amp : 0.0f;
       else
         iapp = a.stim_table[(size_t)t * np + cell];
-      cell_step(a.P, cs, ic, iapp);
-      a.vd[(step + 1) & 1][cell] = cs.Vd;
-      vown[tid] = cs.Vd;
+      Currents cur;
+      cur.I_h = sI[0 * cap + tid];
+      cur.I_CaH = sI[1 * cap + tid];
+      cur.I_K_Ca = sI[2 * cap + tid];
+      cur.I_CaL = sI[3 * cap + tid];
+      cur.I_Na_s = sI[4 * cap + tid];
+      cur.I_Kdr_s = sI[5 * cap + tid];
+      cur.I_K_s = sI[6 * cap + tid];
+      cur.I_Na_a = sI[7 * cap + tid];
+      cur.I_K_a = sI[8 * cap + tid];
+      Volts v;
+      v.Vd = sVd[tid];
+      v.Vs = sVs[tid];
+      v.Va = sVa[tid];
+      voltage_step(a.P, v, cur, ic, iapp);
+      if (LL)
+        st_relaxed_gpu_u64(a.vll[(step + 1) & 1] + cell, pack_stamp(v.Vd, (unsigned)(step + 1)));
+      else
+        a.vd[(step + 1) & 1][cell] = v.Vd;
+      sVd[tid] = v.Vd;
+      sVs[tid] = v.Vs;
+      sVa[tid] = v.Va;
       if (a.trace_every > 0 && (step % a.trace_every) == 0) {
         float* tr = a.trace + (size_t)row * a.trace_nq * np + cell;
         int qi = 0;
-        if (a.trace_mask & TRACE_AXON) tr[(qi++) * np] = cs.Va;
-        if (a.trace_mask & TRACE_SOMA) tr[(qi++) * np] = cs.Vs;
-        if (a.trace_mask & TRACE_DEND) tr[(qi++) * np] = cs.Vd;
+        if (a.trace_mask & TRACE_AXON) tr[(qi++) * np] = v.Va;
+        if (a.trace_mask & TRACE_SOMA) tr[(qi++) * np] = v.Vs;
+        if (a.trace_mask & TRACE_DEND) tr[(qi++) * np] = v.Vd;
       }
     }
     if (a.trace_every > 0 && (step % a.trace_every) == 0) ++row;
 
-    if (t + 1 < a.n_steps) {
+    if (LL) {
+      uint64_t t_arrive = prof ? globaltimer_ns() : 0;
+      __syncthreads();  // new voltages / free tile buffers before the next step
+      if (prof) {
+        const uint64_t t_done = globaltimer_ns();
+        s_prof[0] += t_ready - t_step;
+        s_prof[1] += t_coupled - t_ready;
+        s_prof[2] += t_arrive - t_coupled;
+        s_prof[3] += t_done - t_arrive;
+        s_prof[4] += 1;
+        t_step = t_done;
+      }
+    } else if (t + 1 < a.n_steps) {
       bar_target += gridDim.x;
       uint64_t t_arrive = 0;
       const bool ok = grid_sync(a, bar_target, &s_abort, prof ? &t_arrive : nullptr);
@@ -338,32 +570,47 @@ __global__ void __launch_bounds__(1024, 1) step_kernel(const __grid_constant__ S
     atomicAdd(pr + PROF_BARRIER, s_prof[3]);
     atomicAdd(pr + PROF_STEPS, s_prof[4]);
   }
+  __syncthreads();
 
-  if (owner) {
+  if (unit_lane) {
+    const int c = w.cell_begin + ucell_l;
     float* st = a.st;
-    st[F_VS * np + cell] = cs.Vs;
-    st[F_VA * np + cell] = cs.Va;
-    st[F_Q * np + cell] = cs.q;
-    st[F_R * np + cell] = cs.r;
-    st[F_S * np + cell] = cs.s;
-    a.ca[cell] = cs.Ca;
-    st[F_ICAH * np + cell] = cs.ICaH;
-    st[F_K * np + cell] = cs.k;
-    st[F_L * np + cell] = cs.l;
-    st[F_M * np + cell] = cs.m;
-    st[F_H * np + cell] = cs.h;
-    st[F_N * np + cell] = cs.n;
-    st[F_P * np + cell] = cs.p;
-    st[F_XS * np + cell] = cs.xs;
-    st[F_MA * np + cell] = cs.ma;
-    st[F_HA * np + cell] = cs.ha;
-    st[F_XA * np + cell] = cs.xa;
+    if (umask & 0x01u) st[F_Q * np + c] = gs.q;
+    if (umask & 0x02u) {
+      st[F_R * np + c] = gs.r;
+      st[F_S * np + c] = gs.s;
+      a.ca[c] = gs.Ca;
+      st[F_ICAH * np + c] = gs.ICaH;
+    }
+    if (umask & 0x04u) {
+      st[F_K * np + c] = gs.k;
+      st[F_L * np + c] = gs.l;
+    }
+    if (umask & 0x08u) {
+      st[F_M * np + c] = gs.m;
+      st[F_H * np + c] = gs.h;
+    }
+    if (umask & 0x10u) {
+      st[F_N * np + c] = gs.n;
+      st[F_P * np + c] = gs.p;
+    }
+    if (umask & 0x20u) st[F_XS * np + c] = gs.xs;
+    if (umask & 0x40u) {
+      st[F_MA * np + c] = gs.ma;
+      st[F_HA * np + c] = gs.ha;
+    }
+    if (umask & 0x80u) st[F_XA * np + c] = gs.xa;
+  }
+  if (owner) {
+    if (LL) a.vd[(a.step0 + a.n_steps) & 1][cell] = sVd[tid];
+    a.st[F_VS * np + cell] = sVs[tid];
+    a.st[F_VA * np + cell] = sVa[tid];
   }
 }
 
-template <bool K, bool G>
+template <bool K, bool G, bool LL>
 cudaError_t launch_variant(const StepArgs& a, int grid, int threads, size_t smem, cudaStream_t stream) {
-  auto fn = step_kernel<K, G>;
+  auto fn = step_kernel<K, G, LL>;
   cudaError_t e = cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
   if (e != cudaSuccess) return e;
   void* args[] = {const_cast<StepArgs*>(&a)};
@@ -378,17 +625,23 @@ cudaError_t launch_step_kernel(const StepArgs& a, int grid, int threads, cudaStr
   const size_t smem = step_kernel_smem(a);
   const bool g = a.edge_g != nullptr;
   if (threads != a.shape.threads) return cudaErrorInvalidValue;
-  if (a.shape.kahan) return g ? launch_variant<true, true>(a, grid, threads, smem, stream)
-                        : launch_variant<true, false>(a, grid, threads, smem, stream);
-  return g ? launch_variant<false, true>(a, grid, threads, smem, stream)
-           : launch_variant<false, false>(a, grid, threads, smem, stream);
+  if (a.shape.stamped) {
+    if (a.shape.kahan) return g ? launch_variant<true, true, true>(a, grid, threads, smem, stream)
+                                : launch_variant<true, false, true>(a, grid, threads, smem, stream);
+    return g ? launch_variant<false, true, true>(a, grid, threads, smem, stream)
+             : launch_variant<false, false, true>(a, grid, threads, smem, stream);
+  }
+  if (a.shape.kahan) return g ? launch_variant<true, true, false>(a, grid, threads, smem, stream)
+                              : launch_variant<true, false, false>(a, grid, threads, smem, stream);
+  return g ? launch_variant<false, true, false>(a, grid, threads, smem, stream)
+           : launch_variant<false, false, false>(a, grid, threads, smem, stream);
 }
 
 int max_coresident_ctas(int threads, size_t smem) {
   int dev = 0, nsm = 0, per_sm = 0;
   cudaGetDevice(&dev);
   cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev);
-  auto fn = step_kernel<false, false>;
+  auto fn = step_kernel<false, false, false>;
   cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
   if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, fn, threads, smem) != cudaSuccess) return 0;
   return per_sm * nsm;

@@ -21,7 +21,13 @@ enum StimKind { STIM_PULSE = 0, STIM_CELL = 1, STIM_TABLE = 2 };
 enum TraceBits { TRACE_AXON = 1, TRACE_SOMA = 2, TRACE_DEND = 4 };
 
 // Error codes written by the device into *err (0 = fine).
-enum DevError { DEV_OK = 0, DEV_ERR_BARRIER_TIMEOUT = 1, DEV_ERR_COPY_TIMEOUT = 2, DEV_ERR_CONFIG = 3 };
+enum DevError {
+  DEV_OK = 0,
+  DEV_ERR_BARRIER_TIMEOUT = 1,
+  DEV_ERR_COPY_TIMEOUT = 2,
+  DEV_ERR_CONFIG = 3,
+  DEV_ERR_STAMP_TIMEOUT = 4
+};
 
 struct StepArgs {
   ModelParams P;
@@ -36,6 +42,10 @@ struct StepArgs {
   float g_uniform;            // used when edge_g and cell_g are both null
   // state
   float* vd[2];               // V_dend double buffer, V^step in vd[step & 1]
+  unsigned long long* vll[2]; // stamped mode: (step << 32 | V_dend bits) per cell, slot step & 1
+  const int* probes;          // stamped mode: progress-probe cells (CtaWork::probe_begin..)
+  const int2* gdesc;          // stamped mode: {slot, recv} per lane-chunk (32 per group)
+  int n_cells;                // cells in the network (stamped words >= n_cells are never written)
   float* st;                  // F_COUNT x n_pad floats
   double* ca;                 // Ca2Plus, n_pad doubles
   long long n_pad;

@@ -14,6 +14,16 @@
 //     update thread adds its receiver's slots in sender order.
 // Edge entries are 16-bit offsets from the tile start (a tile is at most
 // 65536 floats), so one gather from shared memory per edge.
+//
+// Two ways of exchanging V_dend between steps:
+//   * barrier mode: V_dend double buffer in global memory, one grid barrier
+//     per step, tiles staged by bulk async copies (any window size);
+//   * stamped mode (all of a CTA's tiles fit in shared memory at once): every
+//     cell publishes (V_dend, step) as one 64-bit word into a two-slot array;
+//     a CTA polls exactly the words it reads (plus one word of every CTA that
+//     reads it without being read by it, so no slot is overwritten before its
+//     readers are done) until their stamps show the step it needs.  No grid
+//     barrier: each CTA waits only for its own neighbourhood.
 #pragma once
 #include <stddef.h>
 #include <stdint.h>
@@ -24,6 +34,15 @@ namespace infoli {
 
 enum { kChunkEdges = 128 };
 
+// Packed layout of stamped plans.  A lane-chunk is up to kLaneEdges edges of
+// one receiver reduced by ONE lane; 32 lane-chunks form a group handled by
+// one warp.  Entries are stored transposed in 4-entry quads so lane l reads
+// its next four entries with one 8-byte load:
+//   entry k of lane l in group g at ((g * kQuads + k / 4) * 32 + l) * 4 + k % 4
+// Each entry is the byte offset, from the start of dynamic shared memory, of
+// the sender's V_dend; padding entries address the receiver's own V_dend.
+enum { kLaneEdges = 32, kQuads = kLaneEdges / 4, kGroupEntries = 32 * kLaneEdges };
+
 typedef struct {
   int cell_begin;   // first owned cell (index into the V_dend / state arrays)
   int n_cells;      // owned cells, <= threads per CTA
@@ -31,6 +50,10 @@ typedef struct {
   int n_tiles;      // tiles this CTA stages each step
   int slot_begin;   // partial slots of this CTA: chunk ids slot_begin.. (absolute)
   int n_slots;      // number of chunks == number of partial slots
+  int probe_begin;  // stamped-exchange mode: cells of CTAs that read this CTA's
+  int n_probes;     //   cells but are not read by it (progress probes)
+  int group_begin;  // stamped mode: first lane-chunk group of this CTA (absolute)
+  int n_groups;     //   number of groups
   int pad0, pad1;
 } CtaWork;
 
@@ -42,9 +65,10 @@ typedef struct {
 } TileDesc;
 
 typedef struct {
+  int slot;         // partial slot, relative to the CTA's slot_begin (first: the
+  int recv;         //   kernel loads {slot, recv} as one 8-byte word)
+                    // receiver, relative to the CTA's cell_begin
   int edge_begin;   // absolute index into the edge-offset (and per-edge g) arrays
-  int slot;         // partial slot, relative to the CTA's slot_begin
-  int recv;         // receiver, relative to the CTA's cell_begin
   int count;        // edges in this chunk, 1..kChunkEdges
 } ChunkDesc;
 
@@ -63,16 +87,23 @@ typedef struct {
   int tile_cap;    // floats per tile buffer
   int nbuf;        // tile buffers (1 or 2)
   int threads;     // threads per CTA
+  int cells_cap;   // owned cells per CTA (max over CTAs, multiple of 32)
   int max_slots;   // partial-sum slots per CTA
   int kahan;       // compensated sums (second slot array)
   int res_tiles;   // resident tile descriptors per CTA (0: not resident)
-  int res_chunks;  // resident chunk descriptors per CTA
+  int res_chunks;  // resident chunk descriptors per CTA (stamped: lane-chunks, 16 B each)
   int res_edges;   // resident edge offsets per CTA
   int edge_g;      // per-edge conductances present
+  int stamped;     // stamped exchange (all tiles resident at once, nbuf = 1)
 } SmemShape;
 
+// Number of per-cell float arrays kept in shared memory: V_dend, V_soma,
+// V_axon and the nine gate-unit currents.
+enum { kCellArrays = 12 };
+
 // Dynamic shared-memory layout of the step kernel (byte offsets):
-//   [tile buffers: nbuf x tile_cap floats][own V_dend: threads floats]
+//   [tile buffers: nbuf x tile_cap floats]
+//   [cell arrays: kCellArrays x cells_cap floats]
 //   [partial sums: max_slots floats][Kahan compensations: max_slots floats]
 //   [2 mbarriers, 16-byte aligned]
 //   resident plans only: [tile descs][chunk descs][per-edge g][edge offsets]
@@ -86,7 +117,7 @@ static inline INFOLI_HD SmemLayout smem_layout(SmemShape s) {
   L.tiles = off;
   off += (size_t)s.nbuf * (size_t)s.tile_cap * sizeof(float);
   L.vown = off;
-  off += (size_t)s.threads * sizeof(float);
+  off += (size_t)kCellArrays * (size_t)s.cells_cap * sizeof(float);
   L.part = off;
   off += (size_t)s.max_slots * sizeof(float);
   L.partc = off;

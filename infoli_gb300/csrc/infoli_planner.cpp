@@ -2,16 +2,18 @@
 #include "infoli_planner.h"
 
 #include <algorithm>
+#include <cmath>
 #include <cstdio>
 #include <numeric>
 
 namespace infoli {
 
-size_t plan_smem_bytes(int tile_cap, int nbuf, int threads, int max_slots, int kahan) {
+size_t plan_smem_bytes(int tile_cap, int nbuf, int threads, int cells_cap, int max_slots, int kahan) {
   SmemShape s{};
   s.tile_cap = tile_cap;
   s.nbuf = nbuf;
   s.threads = threads;
+  s.cells_cap = cells_cap;
   s.max_slots = max_slots;
   s.kahan = kahan;
   return smem_layout(s).total;
@@ -84,6 +86,122 @@ std::vector<TileSpan> make_tiles(const std::vector<int>& u, int cap, int n_pad) 
   return t;
 }
 
+// Build the packed lane-chunk tables of a stamped, resident plan (see
+// infoli_plan.h): per receiver, its senders (ascending) become byte offsets
+// into the CTA's concatenated tiles, cut into lane-chunks of kLaneEdges;
+// the chunks of a CTA, receiver-major, are dealt 32 per group.  Inside a
+// group, entries are permuted per chunk so that the 32 lanes reading
+// position k hit distinct shared-memory banks where possible.  Receiver slots
+// are rewritten to the lane-chunks (receiver-major, so a receiver's partial
+// sums stay contiguous and in sender order); the last group of a CTA is
+// filled with dummy chunks that write one spare slot.
+void pack_groups(Plan& P, const SmemLayout& L, const PlanInput& in, const std::vector<int>& starts) {
+  const bool edge_g = in.g != nullptr;
+  std::vector<int2_t> gdesc;
+  std::vector<uint16_t> pe;
+  std::vector<float> pg;
+  int max_slots = 1;
+  for (size_t b = 0; b < P.cta.size(); ++b) {
+    CtaWork& w = P.cta[b];
+    // tile table of this CTA with offsets into the concatenated buffer
+    std::vector<int> tlo, thi, toff;
+    int off = 0;
+    for (int j = 0; j < w.n_tiles; ++j) {
+      const TileDesc& td = P.tiles[w.tile_begin + j];
+      tlo.push_back(td.lo);
+      thi.push_back(td.lo + td.nfloats);
+      toff.push_back(off);
+      off += td.nfloats;
+    }
+    struct LaneChunk {
+      int recv, slot;
+      std::vector<std::pair<uint16_t, float>> e;
+    };
+    std::vector<LaneChunk> lc;
+    int slot = 0;
+    for (int r = 0; r < w.n_cells; ++r) {
+      const int c = w.cell_begin + r;
+      std::vector<std::pair<int, float>> snd;
+      for (int64_t e = in.row_ptr[c]; e < in.row_ptr[c + 1]; ++e) snd.push_back({in.col[e], edge_g ? in.g[e] : 0.0f});
+      std::stable_sort(snd.begin(), snd.end(),
+                       [](const std::pair<int, float>& x, const std::pair<int, float>& y) { return x.first < y.first; });
+      P.cell_slots[c].begin = slot;
+      size_t j = 0;
+      for (size_t k = 0; k < snd.size(); k += kLaneEdges) {
+        LaneChunk ch;
+        ch.recv = r;
+        ch.slot = slot++;
+        for (size_t q = k; q < std::min(snd.size(), k + kLaneEdges); ++q) {
+          const int s = snd[q].first;
+          while (s >= thi[j]) ++j;
+          ch.e.push_back({(uint16_t)(L.tiles + sizeof(float) * (size_t)(toff[j] + s - tlo[j])), snd[q].second});
+        }
+        lc.push_back(std::move(ch));
+      }
+      P.cell_slots[c].count = slot - P.cell_slots[c].begin;
+    }
+    const int dummy_slot = slot;
+    w.n_slots = slot;
+    max_slots = std::max(max_slots, slot + 1);
+    const int ng = (int)(lc.size() + 31) / 32;
+    w.group_begin = (int)(gdesc.size() / 32);
+    w.n_groups = ng;
+    for (int g = 0; g < ng; ++g) {
+      // the 32 chunks of this group (dummies past the end)
+      std::vector<std::vector<std::pair<uint16_t, float>>> rem(32);
+      std::vector<uint16_t> pad(32);
+      for (int l = 0; l < 32; ++l) {
+        const size_t ci = (size_t)g * 32 + l;
+        int2_t d;
+        if (ci < lc.size()) {
+          d.x = lc[ci].slot;
+          d.y = lc[ci].recv;
+          rem[l] = lc[ci].e;
+        } else {
+          d.x = dummy_slot;
+          d.y = 0;
+        }
+        pad[l] = (uint16_t)(L.vown + sizeof(float) * (size_t)d.y);
+        gdesc.push_back(d);
+      }
+      // greedy bank-distinct dealing, position by position
+      std::vector<std::pair<uint16_t, float>> cell(32 * kLaneEdges);
+      for (int k = 0; k < kLaneEdges; ++k) {
+        unsigned used = 0;
+        for (int l = 0; l < 32; ++l) {
+          std::pair<uint16_t, float> pick = {pad[l], 0.0f};
+          if (!rem[l].empty()) {
+            size_t best = rem[l].size() - 1;
+            for (size_t q = 0; q < rem[l].size(); ++q)
+              if (!((used >> ((rem[l][q].first >> 2) & 31)) & 1u)) {
+                best = q;
+                break;
+              }
+            pick = rem[l][best];
+            rem[l].erase(rem[l].begin() + best);
+          }
+          used |= 1u << ((pick.first >> 2) & 31);
+          cell[l * kLaneEdges + k] = pick;
+        }
+      }
+      // transposed quads: ((g * kQuads + k / 4) * 32 + l) * 4 + k % 4
+      const size_t base = pe.size();
+      pe.resize(base + kGroupEntries);
+      if (edge_g) pg.resize(base + kGroupEntries);
+      for (int l = 0; l < 32; ++l)
+        for (int k = 0; k < kLaneEdges; ++k) {
+          const size_t at = base + ((size_t)(k / 4) * 32 + l) * 4 + (k % 4);
+          pe[at] = cell[l * kLaneEdges + k].first;
+          if (edge_g) pg[at] = cell[l * kLaneEdges + k].second;
+        }
+    }
+  }
+  P.gdesc.swap(gdesc);
+  P.edges.swap(pe);
+  P.edge_g.swap(pg);
+  P.max_slots = max_slots;
+}
+
 }  // namespace
 
 bool make_plan(const PlanInput& in, Plan* out, std::string* err) {
@@ -131,6 +249,8 @@ bool make_plan(const PlanInput& in, Plan* out, std::string* err) {
   }
   std::vector<int> starts = partition_cells(n, in.row_ptr, grid, threads);
   const int ctas = (int)starts.size() - 1;
+  int cells_cap = 32;
+  for (int b = 0; b < ctas; ++b) cells_cap = std::max(cells_cap, ((starts[b + 1] - starts[b] + 31) / 32) * 32);
 
   // ---- per-CTA sorted edges (sender, g) and unique sender lists
   std::vector<std::vector<int>> uniq(ctas);
@@ -176,9 +296,9 @@ bool make_plan(const PlanInput& in, Plan* out, std::string* err) {
       max_slots = std::max(max_slots, slots_for(b, tiles[b]));
     }
     max_slots = std::max(max_slots, 1);
-    if (plan_smem_bytes(tile_cap, nbuf, threads, max_slots, in.kahan) <= in.smem_budget) break;
+    if (plan_smem_bytes(tile_cap, nbuf, threads, cells_cap, max_slots, in.kahan) <= in.smem_budget) break;
     // shrink: give the tiles what is left after the fixed part
-    size_t fixed = plan_smem_bytes(0, 0, threads, max_slots, in.kahan);
+    size_t fixed = plan_smem_bytes(0, 0, threads, cells_cap, max_slots, in.kahan);
     size_t avail = in.smem_budget > fixed ? in.smem_budget - fixed : 0;
     int cap = (int)std::min<size_t>(avail / (2 * sizeof(float)), (size_t)tile_cap * 3 / 4);
     cap &= ~3;
@@ -189,7 +309,7 @@ bool make_plan(const PlanInput& in, Plan* out, std::string* err) {
     tile_cap = cap;
     nbuf = 2;
   }
-  if (plan_smem_bytes(tile_cap, nbuf, threads, max_slots, in.kahan) > in.smem_budget) {
+  if (plan_smem_bytes(tile_cap, nbuf, threads, cells_cap, max_slots, in.kahan) > in.smem_budget) {
     *err = "make_plan: could not fit shared memory";
     return false;
   }
@@ -202,7 +322,7 @@ bool make_plan(const PlanInput& in, Plan* out, std::string* err) {
   P.tile_cap = tile_cap;
   P.nbuf = nbuf;
   P.max_slots = max_slots;
-  P.smem_bytes = plan_smem_bytes(tile_cap, nbuf, threads, max_slots, in.kahan);
+  P.smem_bytes = plan_smem_bytes(tile_cap, nbuf, threads, cells_cap, max_slots, in.kahan);
   P.cell_slots.assign(n, CellSlots{0, 0});
   P.edges.reserve(E);
   if (in.g) P.edge_g.reserve(E);
@@ -281,6 +401,7 @@ bool make_plan(const PlanInput& in, Plan* out, std::string* err) {
   sh.tile_cap = tile_cap;
   sh.nbuf = nbuf;
   sh.threads = threads;
+  sh.cells_cap = cells_cap;
   sh.max_slots = max_slots;
   sh.kahan = in.kahan;
   sh.edge_g = in.g ? 1 : 0;
@@ -299,9 +420,178 @@ bool make_plan(const PlanInput& in, Plan* out, std::string* err) {
   res.res_chunks = std::max(mc, 1);
   res.res_edges = std::max(me, 1);
   if (!in.no_resident && smem_layout(res).total <= in.smem_budget) sh = res;
+
+  // ---- stamped exchange when every CTA's tiles fit in shared memory at once
+  if (in.sync_mode != kSyncBarrier) {
+    int sum_max = 4;
+    for (const CtaWork& w : P.cta) {
+      int s = 0;
+      for (int j = 0; j < w.n_tiles; ++j) s += P.tiles[w.tile_begin + j].nfloats;
+      sum_max = std::max(sum_max, s);
+    }
+    // stamped plans keep their work resident in the packed lane-chunk layout,
+    // 16-bit byte offsets from the start of dynamic shared memory (so every
+    // offset must stay below 64 KiB)
+    SmemShape st = sh;
+    st.tile_cap = (sum_max + 3) & ~3;
+    st.nbuf = 1;
+    st.stamped = 1;
+    const SmemLayout SL0 = smem_layout(st);  // tile and cell-array offsets do not depend on the rest
+    const bool offsets_fit = SL0.vown + sizeof(float) * (size_t)cells_cap <= 65536;
+    Plan packed = P;
+    bool fits = false;
+    if (!in.no_resident && offsets_fit) {
+      pack_groups(packed, SL0, in, starts);
+      int mg = 1;
+      for (const CtaWork& w : packed.cta) mg = std::max(mg, w.n_groups);
+      st.max_slots = packed.max_slots;
+      st.res_tiles = std::max(mt, 1);
+      st.res_chunks = mg * 32;
+      st.res_edges = mg * kGroupEntries;
+      fits = smem_layout(st).total <= in.smem_budget;
+    }
+    if (fits) {
+      sh = st;
+      P.cta.swap(packed.cta);
+      P.cell_slots.swap(packed.cell_slots);
+      P.gdesc.swap(packed.gdesc);
+      P.edges.swap(packed.edges);
+      P.edge_g.swap(packed.edge_g);
+      P.max_slots = packed.max_slots;
+      // progress probes: CTAs that read a CTA's cells without being read by it
+      std::vector<int> owner(n);
+      for (int b = 0; b < ctas; ++b)
+        for (int c = starts[b]; c < starts[b + 1]; ++c) owner[c] = b;
+      std::vector<std::vector<char>> reads(ctas, std::vector<char>(ctas, 0));  // reads[r][x]: r polls x
+      for (int b = 0; b < ctas; ++b) {
+        const CtaWork& w = P.cta[b];
+        for (int j = 0; j < w.n_tiles; ++j) {
+          const TileDesc& td = P.tiles[w.tile_begin + j];
+          for (int c = td.lo; c < td.lo + td.nfloats && c < n;) {
+            const int x = owner[c];
+            reads[b][x] = 1;
+            c = starts[x + 1];  // skip to the next owner
+          }
+        }
+      }
+      for (int x = 0; x < ctas; ++x) {
+        CtaWork& w = P.cta[x];
+        w.probe_begin = (int)P.probes.size();
+        for (int r = 0; r < ctas; ++r)
+          if (r != x && reads[r][x] && !reads[x][r]) P.probes.push_back(starts[r]);
+        w.n_probes = (int)P.probes.size() - w.probe_begin;
+      }
+    } else if (in.sync_mode == kSyncStamped) {
+      *err = "make_plan: stamped exchange requested but the tiles do not fit in shared memory";
+      return false;
+    }
+  }
   P.shape = sh;
   P.smem_bytes = smem_layout(sh).total;
   return true;
 }
 
 }  // namespace infoli
+
+// ---------------------------------------------------------------------------
+// Host emulation of a plan: plans a network exactly as infoli_sim_create
+// would for the given launch limits, then evaluates the gap-junction
+// currents by walking the plan's tables with the step kernel's addressing
+// (tile staging, byte offsets into the shared-memory image, padding entries,
+// partial slots).  Every shared-memory offset is bounds-checked.  Used by the
+// CPU test suite to validate the planner without a GPU.
+extern "C" int infoli_plan_emulate(int n, const int64_t* row_ptr, const int32_t* col, const float* g,
+                                   float g_uniform, int grid, int grid_max, int threads, int64_t smem_budget,
+                                   int sync_mode, const float* vdend, float* ic_out, int64_t info[8]) {
+  using namespace infoli;
+  PlanInput in;
+  in.n = n;
+  in.row_ptr = row_ptr;
+  in.col = col;
+  in.g = g;
+  in.grid = grid;
+  in.grid_max = grid_max;
+  in.threads = threads;
+  in.smem_budget = (size_t)smem_budget;
+  in.sync_mode = sync_mode;
+  Plan P;
+  std::string err;
+  if (!make_plan(in, &P, &err)) return -1;
+  const SmemLayout L = smem_layout(P.shape);
+  if (L.total > (size_t)smem_budget) return -2;
+  auto fexp = [](float V) { return 0.8f * std::exp(-(V * V) / 100.0f) + 0.2f; };
+  std::vector<unsigned char> sm(L.total);
+  int64_t groups = 0, probes = 0;
+  for (const CtaWork& w : P.cta) {
+    if (w.n_cells > threads || w.n_cells > P.shape.cells_cap) return -3;
+    std::fill(sm.begin(), sm.end(), 0);
+    float* fsm = reinterpret_cast<float*>(sm.data());
+    std::vector<float> part(P.shape.max_slots, 0.0f);
+    float* sVd = reinterpret_cast<float*>(sm.data() + L.vown);
+    for (int r = 0; r < w.n_cells; ++r) sVd[r] = vdend[w.cell_begin + r];
+    if (P.shape.stamped) {
+      size_t toff = 0;
+      for (int j = 0; j < w.n_tiles; ++j) {
+        const TileDesc& td = P.tiles[w.tile_begin + j];
+        if (td.lo < 0 || td.lo % 4 || td.nfloats % 4 || toff + td.nfloats > (size_t)P.shape.tile_cap) return -4;
+        for (int i = 0; i < td.nfloats; ++i) fsm[toff + i] = (td.lo + i < n) ? vdend[td.lo + i] : 0.0f;
+        toff += td.nfloats;
+      }
+      for (int q = 0; q < w.n_probes; ++q)
+        if (P.probes[w.probe_begin + q] < 0 || P.probes[w.probe_begin + q] >= n) return -5;
+      probes += w.n_probes;
+      groups += w.n_groups;
+      for (int gi = 0; gi < w.n_groups; ++gi)
+        for (int l = 0; l < 32; ++l) {
+          const int2_t d = P.gdesc[((size_t)w.group_begin + gi) * 32 + l];
+          if (d.x < 0 || d.x >= P.shape.max_slots || d.y < 0 || d.y >= std::max(w.n_cells, 1)) return -6;
+          const float vc = sVd[d.y];
+          float acc0 = 0.0f, acc1 = 0.0f;
+          for (int k = 0; k < kLaneEdges; ++k) {
+            const size_t at = (((size_t)w.group_begin + gi) * kQuads + k / 4) * 32 * 4 + (size_t)l * 4 + k % 4;
+            const unsigned off = P.edges[at];
+            if (off % 4 || off + 4 > L.vown + sizeof(float) * (size_t)P.shape.cells_cap) return -7;
+            const float V = vc - *reinterpret_cast<const float*>(sm.data() + off);
+            const float gg = g ? P.edge_g[at] : 1.0f;
+            ((k & 1) ? acc1 : acc0) += (gg * fexp(V)) * V;
+          }
+          part[d.x] = acc0 + acc1;
+        }
+    } else {
+      for (int j = 0; j < w.n_tiles; ++j) {
+        const TileDesc& td = P.tiles[w.tile_begin + j];
+        if (td.lo < 0 || td.lo % 4 || td.nfloats % 4 || td.nfloats > P.shape.tile_cap) return -4;
+        for (int ci = td.chunk_begin; ci < td.chunk_end; ++ci) {
+          const ChunkDesc& c = P.chunks[ci];
+          if (c.slot < 0 || c.slot >= P.shape.max_slots || c.recv < 0 || c.recv >= w.n_cells) return -6;
+          float acc = 0.0f;
+          for (int k = 0; k < c.count; ++k) {
+            const int o = P.edges[c.edge_begin + k];
+            if (o >= td.nfloats || td.lo + o >= n) return -7;
+            const float V = sVd[c.recv] - vdend[td.lo + o];
+            acc += (g ? P.edge_g[c.edge_begin + k] : 1.0f) * fexp(V) * V;
+          }
+          part[c.slot] = acc;
+        }
+      }
+      groups += P.tiles.empty() ? 0 : 0;
+    }
+    for (int r = 0; r < w.n_cells; ++r) {
+      const CellSlots cs = P.cell_slots[w.cell_begin + r];
+      float ic = 0.0f;
+      for (int q = 0; q < cs.count; ++q) ic += part[cs.begin + q];
+      ic_out[w.cell_begin + r] = g ? ic : ic * g_uniform;
+    }
+  }
+  if (info) {
+    info[0] = P.grid;
+    info[1] = P.shape.stamped;
+    info[2] = (int64_t)P.tiles.size();
+    info[3] = P.shape.stamped ? groups : (int64_t)P.chunks.size();
+    info[4] = P.shape.max_slots;
+    info[5] = (int64_t)P.smem_bytes;
+    info[6] = probes;
+    info[7] = P.shape.res_chunks > 0;
+  }
+  return 0;
+}

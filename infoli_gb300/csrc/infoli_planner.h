@@ -14,6 +14,10 @@ namespace infoli {
 // 32 spare entries, so tile ends rounded up to 16 bytes stay in bounds.
 inline int pad_cells(int n) { return ((n + 31) / 32) * 32 + 32; }
 
+struct alignas(8) int2_t {
+  int x, y;
+};
+
 struct alignas(8) CellSlots {
   int begin;  // first partial slot, relative to the CTA
   int count;  // number of slots (chunks) of this receiver
@@ -30,7 +34,10 @@ struct PlanInput {
   size_t smem_budget = 0;          // dynamic shared memory per CTA (bytes)
   int kahan = 0;
   int no_resident = 0;             // force per-step reads of the static work from global memory
+  int sync_mode = 0;               // kSyncAuto / kSyncBarrier / kSyncStamped
 };
+
+enum { kSyncAuto = 0, kSyncBarrier = 1, kSyncStamped = 2 };
 
 struct Plan {
   int grid = 0, threads = 0, tile_cap = 0, nbuf = 1, max_slots = 0;
@@ -42,10 +49,12 @@ struct Plan {
   std::vector<CellSlots> cell_slots;  // [n]
   std::vector<uint16_t> edges;
   std::vector<float> edge_g;          // empty unless per-edge g
+  std::vector<int> probes;            // stamped mode: progress-probe cells
+  std::vector<int2_t> gdesc;          // stamped mode: {slot, recv} per lane-chunk, 32 per group
 };
 
 // Shared-memory bytes the step kernel needs for a plan's parameters.
-size_t plan_smem_bytes(int tile_cap, int nbuf, int threads, int max_slots, int kahan);
+size_t plan_smem_bytes(int tile_cap, int nbuf, int threads, int cells_cap, int max_slots, int kahan);
 
 // Returns false and sets *err on failure.
 bool make_plan(const PlanInput& in, Plan* out, std::string* err);

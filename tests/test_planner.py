@@ -1,0 +1,94 @@
+"""The work planner, checked on the CPU: every plan the step kernel would run
+is walked with the kernel's addressing (infoli_plan_emulate) and must give the
+gap-junction currents of the CSR network, for both V_dend exchange modes."""
+import numpy as np
+import pytest
+
+from helpers import kat_topology
+
+
+@pytest.fixture(scope="module")
+def capi(built):
+    from infoli_gb300 import capi
+
+    return capi
+
+
+def direct_ic(n, rp, col, v, g=None, g_uniform=0.04):
+    v = v.astype(np.float64)
+    out = np.zeros(n)
+    for r in range(n):
+        s = col[rp[r]:rp[r + 1]]
+        V = v[r] - v[s]
+        w = g[rp[r]:rp[r + 1]].astype(np.float64) if g is not None else g_uniform
+        out[r] = np.sum(w * (0.8 * np.exp(-V * V / 100) + 0.2) * V)
+    return out
+
+
+def check(capi, n, rp, col, g=None, sync_mode=0, seed=0, **kw):
+    rng = np.random.default_rng(seed)
+    v = (-60 + rng.uniform(-15, 15, n)).astype(np.float32)
+    ic, info = capi.plan_emulate(n, rp, col, v, g=g, sync_mode=sync_mode, **kw)
+    ref = direct_ic(n, rp, col, v, g)
+    scale = np.maximum(1.0, np.abs(ref))
+    assert np.max(np.abs(ic - ref) / scale) < 2e-4, info
+    return info
+
+
+@pytest.mark.parametrize("mode", [1, 2])
+def test_kat_network(capi, mode):
+    n, rp, col, g, _ = kat_topology()
+    info = check(capi, n, rp, col, g=g, sync_mode=mode)
+    assert info["stamped"] == (mode == 2)
+
+
+@pytest.mark.parametrize("mode", [1, 2])
+@pytest.mark.parametrize("n,p", [(1, 0.5), (33, 1.0), (1000, 0.1), (3000, 0.02)])
+def test_reference_generator_networks(capi, n, p, mode):
+    rp, col = capi.gen_uniform(n, p, 1)
+    info = check(capi, n, rp, col, sync_mode=mode)
+    assert info["ctas"] >= 1
+
+
+def test_grid_network_10k_stamped(capi):
+    rp, col = capi.gen_grid_gaussian(100, 100, 10.0, 18.0, 1)
+    info = check(capi, 10000, rp, col, sync_mode=0)
+    assert info["stamped"] == 1 and info["resident"] == 1 and info["ctas"] == 152
+
+
+def test_grid_network_barrier_and_small_grids(capi):
+    rp, col = capi.gen_grid_gaussian(40, 50, 6.0, 10.0, 3)
+    for grid in (2, 7, 64):
+        check(capi, 2000, rp, col, sync_mode=1, grid=grid)
+        check(capi, 2000, rp, col, sync_mode=0 if grid < 7 else 2, grid=grid)
+
+
+def test_per_edge_g_stamped_and_barrier(capi):
+    rp, col, g = capi.gen_fixed_degree(5000, 40, 3, (0.02, 0.06))
+    a = check(capi, 5000, rp, col, g=g, sync_mode=2)
+    b = check(capi, 5000, rp, col, g=g, sync_mode=1)
+    assert a["stamped"] == 1 and b["stamped"] == 0
+
+
+def test_large_window_falls_back_to_barrier_tiles(capi):
+    rp, col, g = capi.gen_fixed_degree(90000, 6, 12, (0.02, 0.06))
+    info = check(capi, 90000, rp, col, g=g)
+    assert info["stamped"] == 0 and info["tiles"] > info["ctas"]
+
+
+def test_isolated_cells_and_empty_rows(capi):
+    n = 300
+    rp, col = capi.gen_uniform(n, 0.05, 4)
+    # drop every edge of the first 100 receivers
+    keep = np.ones(col.size, bool)
+    keep[: rp[100]] = False
+    col2 = col[keep]
+    rp2 = np.concatenate([[0] * 101, rp[101:] - rp[100]]).astype(np.int64)
+    for mode in (1, 2):
+        check(capi, n, rp2, col2, sync_mode=mode)
+
+
+def test_stamped_request_that_cannot_fit_is_rejected(capi):
+    rp, col, g = capi.gen_fixed_degree(90000, 6, 12, (0.02, 0.06))
+    with pytest.raises(capi.InfoliError):
+        capi.plan_emulate(90000, rp, col, np.zeros(90000, np.float32), g=g, sync_mode=2)
