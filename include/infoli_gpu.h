@@ -203,12 +203,13 @@ int infoli_sim_plan_info(infoli_sim* s, int* grid, int* threads, int* tiles, int
 /* Device-side phase timers, the counterpart of the reference's -DPROFILING
  * build (src/hybrid/infoli.h:35-36, src/hybrid/infoli.c:637-643,974-1000),
  * which accumulates per-phase wall times.  When enabled, thread 0 of every
- * CTA accumulates global-timer intervals per step: [0] tile staging wait,
- * [1] gap-junction coupling, [2] compartment update (until the whole CTA is
- * done), [3] grid barrier.  get_profile reports ns per step, averaged over
- * CTAs (mean_ns) and the slowest CTA (max_ns), since profiling was enabled. */
+ * CTA accumulates global-timer intervals per step: [0] wait for the
+ * neighbours' V_dend (tile staging / stamped words), [1] gap-junction
+ * coupling, [2] voltage step (until the whole CTA is done), [3] grid barrier,
+ * [4] gate units.  get_profile reports ns per step, averaged over CTAs
+ * (mean_ns) and the slowest CTA (max_ns), since profiling was enabled. */
 int infoli_sim_set_profiling(infoli_sim* s, int on);
-int infoli_sim_get_profile(infoli_sim* s, double mean_ns[4], double max_ns[4]);
+int infoli_sim_get_profile(infoli_sim* s, double mean_ns[5], double max_ns[5]);
 
 int infoli_sim_destroy(infoli_sim* s);
 
@@ -218,12 +219,13 @@ int infoli_sim_destroy(infoli_sim* s);
  * (sync_mode 0 auto, 1 grid barrier, 2 stamped words; grid 0 = automatic),
  * then computes the gap-junction currents of the voltages vdend[n] by walking
  * the plan's tables with the step kernel's addressing, every shared-memory
- * offset bounds-checked.  info[8] = {CTAs, stamped, tiles, chunks or groups,
- * partial slots, shared bytes, progress probes, resident}.  Returns 0 or a
- * negative code naming the violated invariant. */
+ * offset bounds-checked.  info[10] = {CTAs, stamped, tiles, chunks or groups,
+ * partial slots, shared bytes, progress probes, resident, shared-memory
+ * wavefronts of the stamped V_dend gathers, gather instructions}.  Returns 0
+ * or a negative code naming the violated invariant. */
 int infoli_plan_emulate(int n, const int64_t* row_ptr, const int32_t* col, const float* g, float g_uniform,
                         int grid, int grid_max, int threads, int64_t smem_budget, int sync_mode,
-                        const float* vdend, float* ic_out, int64_t info[8]);
+                        const float* vdend, float* ic_out, int64_t info[10]);
 
 /* ------------------------------------------------------------------------ */
 /* trace text (host side)                                                    */

@@ -206,13 +206,14 @@ def plan_emulate(n, row_ptr, col, vdend, g=None, g_uniform=0.04, grid=0, grid_ma
     g = None if g is None else np.ascontiguousarray(g, dtype=np.float32)
     v = np.ascontiguousarray(vdend, dtype=np.float32)
     out = np.zeros(n, dtype=np.float32)
-    info = np.zeros(8, dtype=np.int64)
+    info = np.zeros(10, dtype=np.int64)
     rc = load().infoli_plan_emulate(n, _p(row_ptr), _p(col) if col.size else None, _p(g), float(g_uniform),
                                     grid, grid_max, threads, int(smem_budget), sync_mode, _p(v), _p(out),
                                     _p(info))
     if rc != 0:
         raise InfoliError(rc, f"plan emulation failed with code {rc}")
-    keys = ("ctas", "stamped", "tiles", "chunks", "max_slots", "smem_bytes", "probes", "resident")
+    keys = ("ctas", "stamped", "tiles", "chunks", "max_slots", "smem_bytes", "probes", "resident",
+            "gather_wavefronts", "gathers")
     return out, dict(zip(keys, info.tolist()))
 
 
@@ -328,11 +329,11 @@ class Simulation:
         _check(self._L.infoli_sim_set_profiling(self._h, int(bool(on))))
 
     def get_profile(self):
-        """{"mean"/"max": {"stage","couple","update","barrier"}: ns per step}."""
-        mean = np.zeros(4)
-        mx = np.zeros(4)
+        """{"mean"/"max": {"wait","couple","update","barrier","units"}: ns per step}."""
+        mean = np.zeros(5)
+        mx = np.zeros(5)
         _check(self._L.infoli_sim_get_profile(self._h, _p(mean), _p(mx)))
-        keys = ("stage", "couple", "update", "barrier")
+        keys = ("wait", "couple", "update", "barrier", "units")
         return {"mean": dict(zip(keys, mean.tolist())), "max": dict(zip(keys, mx.tolist()))}
 
     def plan_info(self):

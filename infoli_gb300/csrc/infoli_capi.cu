@@ -261,15 +261,29 @@ int infoli_sim_create(const infoli_sim_desc* d, infoli_sim** out) {
   pin.grid = 0;
   const char* gs = getenv("INFOLI_GRID");
   if (gs) pin.grid = atoi(gs);
-  pin.grid_max = nsm;  // one 1024-thread CTA per SM
-  pin.threads = kThreads;
+  pin.grid_max = nsm;  // one CTA per SM
   pin.smem_budget = (size_t)smem_optin - 1024;  // static shared (abort flag) headroom
   pin.kahan = s->kahan;
   pin.no_resident = getenv("INFOLI_NO_RESIDENT") ? 1 : 0;
   if (const char* sm = getenv("INFOLI_SYNC")) pin.sync_mode = !strcmp(sm, "barrier") ? kSyncBarrier : !strcmp(sm, "stamped") ? kSyncStamped : kSyncAuto;
+  // 512-thread CTAs (128 registers per thread) whenever the network fits in
+  // one cell per thread at that size; 1024 threads for larger networks.
+  // INFOLI_THREADS=512|1024 overrides.
+  int want_threads = 0;
+  if (const char* ts = getenv("INFOLI_THREADS")) want_threads = atoi(ts) == 512 ? 512 : 1024;
   std::string perr;
-  if (!make_plan(pin, &s->plan, &perr)) return fail(infoli__fail(INFOLI_ERR_ARG, "%s", perr.c_str()));
-  const int cores = max_coresident_ctas(kThreads, s->plan.smem_bytes);
+  bool planned = false;
+  for (int threads : {512, kThreads}) {
+    if (want_threads && threads != want_threads) continue;
+    if (!want_threads && threads == 512 && (int64_t)nsm * 512 < s->n) continue;
+    pin.threads = threads;
+    if (make_plan(pin, &s->plan, &perr)) {
+      planned = true;
+      break;
+    }
+  }
+  if (!planned) return fail(infoli__fail(INFOLI_ERR_ARG, "%s", perr.c_str()));
+  const int cores = max_coresident_ctas(s->plan.threads, s->plan.smem_bytes);
   if (cores < s->plan.grid)
     return fail(infoli__fail(INFOLI_ERR_CUDA, "plan needs %d co-resident CTAs, device allows %d", s->plan.grid, cores));
 
@@ -585,18 +599,27 @@ int infoli_sim_set_profiling(infoli_sim* s, int on) {
   return INFOLI_OK;
 }
 
-int infoli_sim_get_profile(infoli_sim* s, double mean_ns[4], double max_ns[4]) {
+int infoli_sim_get_profile(infoli_sim* s, double mean_ns[5], double max_ns[5]) {
   infoli__clear_error();
   if (!s || !s->d_prof) return infoli__fail(INFOLI_ERR_STATE, "profiling is not enabled");
   CK(cudaSetDevice(s->device));
   CK(cudaStreamSynchronize(s->stream));
   std::vector<unsigned long long> h((size_t)s->plan.grid * kProfSlots);
   CK(cudaMemcpy(h.data(), s->d_prof, h.size() * sizeof(unsigned long long), cudaMemcpyDeviceToHost));
-  for (int k = 0; k < 4; ++k) {
+  const int slot_of[5] = {PROF_STAGE, PROF_COUPLE, PROF_UPDATE, PROF_BARRIER, PROF_UNITS};
+  // cycles -> ns with the clock seen over the launches (global timer / SM cycles)
+  double span_ns = 0, span_cy = 0;
+  for (int b = 0; b < s->plan.grid; ++b) {
+    span_ns += (double)h[(size_t)b * kProfSlots + PROF_SPAN_NS];
+    span_cy += (double)h[(size_t)b * kProfSlots + PROF_SPAN_CYCLES];
+  }
+  const double ns_per_cycle = span_cy > 0 ? span_ns / span_cy : 0.0;
+  for (int k = 0; k < 5; ++k) {
     double sum = 0, mx = 0;
     for (int b = 0; b < s->plan.grid; ++b) {
       const unsigned long long steps = h[(size_t)b * kProfSlots + PROF_STEPS];
-      const double v = steps ? (double)h[(size_t)b * kProfSlots + k] / (double)steps : 0.0;
+      const double v =
+          steps ? ns_per_cycle * (double)h[(size_t)b * kProfSlots + slot_of[k]] / (double)steps : 0.0;
       sum += v;
       mx = std::max(mx, v);
     }

@@ -160,21 +160,46 @@ __device__ __forceinline__ void run_units(const ModelParams& P, unsigned mask, c
   if (mask & 0x80u) unit_xa(P, v, g, c);
 }
 
+// Inter-compartment coupling coefficients of the voltage step.  The reference
+// evaluates G_INT / (1 - P1) etc. per cell and step; they depend on the
+// parameters only, so they are evaluated once (same IEEE float operations,
+// hence the same values).  Division by C_M is skipped when C_M == 1 (x / 1 is
+// exactly x), the default.
+struct VoltCoef {
+  float k_sd, k_ds, k_as, k_sa;
+  bool cm_one;
+};
+
+__device__ __forceinline__ VoltCoef volt_coef(const ModelParams& P) {
+  VoltCoef k;
+  k.k_sd = P.G_INT / (1.0f - P.P1);
+  k.k_ds = P.G_INT / P.P1;
+  k.k_as = P.G_INT / (1.0f - P.P2);
+  k.k_sa = P.G_INT / P.P2;
+  k.cm_one = P.C_M == 1.0f;
+  return k;
+}
+
 // Voltage step (:587-592, :635-642, :664-675): currents summed in the
 // reference's order, all from the old voltages.  I_c: gap-junction current.
-__device__ __forceinline__ void voltage_step(const ModelParams& P, Volts& v, const Currents& c, float I_c,
-                                             float iApp) {
+__device__ __forceinline__ void voltage_step(const ModelParams& P, const VoltCoef& k, Volts& v, const Currents& c,
+                                             float I_c, float iApp) {
   const float Vd = v.Vd, Vs = v.Vs, Va = v.Va;
-  const float I_sd = (P.G_INT / (1.0f - P.P1)) * (Vd - Vs);
+  const float I_sd = k.k_sd * (Vd - Vs);
   const float I_ld = P.G_LD * (Vd - P.V_L);
-  const float dVd_dt = (-(c.I_CaH + I_sd + I_ld + c.I_K_Ca + I_c + c.I_h) + iApp) / P.C_M;
-  const float I_ds = (P.G_INT / P.P1) * (Vs - Vd);
+  float dVd_dt = -(c.I_CaH + I_sd + I_ld + c.I_K_Ca + I_c + c.I_h) + iApp;
+  const float I_ds = k.k_ds * (Vs - Vd);
   const float I_ls = P.G_LS * (Vs - P.V_L);
-  const float I_as = (P.G_INT / (1.0f - P.P2)) * (Vs - Va);
-  const float dVs_dt = (-(c.I_CaL + I_ds + I_as + c.I_Na_s + I_ls + c.I_Kdr_s + c.I_K_s)) / P.C_M;
+  const float I_as = k.k_as * (Vs - Va);
+  float dVs_dt = -(c.I_CaL + I_ds + I_as + c.I_Na_s + I_ls + c.I_Kdr_s + c.I_K_s);
   const float I_la = P.G_LA * (Va - P.V_L);
-  const float I_sa = (P.G_INT / P.P2) * (Va - Vs);
-  const float dVa_dt = (-(c.I_K_a + I_sa + I_la + c.I_Na_a)) / P.C_M;
+  const float I_sa = k.k_sa * (Va - Vs);
+  float dVa_dt = -(c.I_K_a + I_sa + I_la + c.I_Na_a);
+  if (!k.cm_one) {
+    dVd_dt = dVd_dt / P.C_M;
+    dVs_dt = dVs_dt / P.C_M;
+    dVa_dt = dVa_dt / P.C_M;
+  }
   v.Vd = P.DELTA * dVd_dt + Vd;
   v.Vs = P.DELTA * dVs_dt + Vs;
   v.Va = P.DELTA * dVa_dt + Va;
@@ -184,7 +209,7 @@ __device__ __forceinline__ void voltage_step(const ModelParams& P, Volts& v, con
 __device__ __forceinline__ void cell_step(const ModelParams& P, Volts& v, Gates& g, float I_c, float iApp) {
   Currents c;
   run_units(P, 0xffu, v, g, c);
-  voltage_step(P, v, c, I_c, iApp);
+  voltage_step(P, volt_coef(P), v, c, I_c, iApp);
 }
 
 }  // namespace infoli

@@ -54,7 +54,7 @@ __device__ __forceinline__ bool grid_sync(const StepArgs& a, unsigned target, vo
                                           uint64_t* t_arrive) {
   __syncthreads();
   if (threadIdx.x == 0) {
-    if (t_arrive) *t_arrive = globaltimer_ns();
+    if (t_arrive) *t_arrive = clock64();
     __threadfence();
     red_release_gpu_add(a.bar, 1u);
     if (ld_acquire_gpu(a.bar) < target) {
@@ -77,6 +77,61 @@ __device__ __forceinline__ bool grid_sync(const StepArgs& a, unsigned target, vo
 }
 
 
+// Gate state of local cell r from / to shared memory (field f at
+// sG[f * cap + r]), only the fields the units in `mask` use.
+__device__ __forceinline__ Gates load_gates(const float* sG, const double* sCa, int cap, int r, unsigned mask) {
+  Gates g;
+  if (mask & 0x01u) g.q = sG[F_Q * cap + r];
+  if (mask & 0x02u) {
+    g.r = sG[F_R * cap + r];
+    g.s = sG[F_S * cap + r];
+    g.Ca = sCa[r];
+    g.ICaH = sG[F_ICAH * cap + r];
+  }
+  if (mask & 0x04u) {
+    g.k = sG[F_K * cap + r];
+    g.l = sG[F_L * cap + r];
+    g.gCaL = sG[F_GCAL * cap + r];
+  }
+  if (mask & 0x08u) g.h = sG[F_H * cap + r];
+  if (mask & 0x10u) {
+    g.n = sG[F_N * cap + r];
+    g.p = sG[F_P * cap + r];
+  }
+  if (mask & 0x20u) g.xs = sG[F_XS * cap + r];
+  if (mask & 0x40u) g.ha = sG[F_HA * cap + r];
+  if (mask & 0x80u) g.xa = sG[F_XA * cap + r];
+  return g;
+}
+
+__device__ __forceinline__ void store_gates(float* sG, double* sCa, int cap, int r, unsigned mask, const Gates& g) {
+  if (mask & 0x01u) sG[F_Q * cap + r] = g.q;
+  if (mask & 0x02u) {
+    sG[F_R * cap + r] = g.r;
+    sG[F_S * cap + r] = g.s;
+    sCa[r] = g.Ca;
+    sG[F_ICAH * cap + r] = g.ICaH;
+  }
+  if (mask & 0x04u) {
+    sG[F_K * cap + r] = g.k;
+    sG[F_L * cap + r] = g.l;
+  }
+  if (mask & 0x08u) {
+    sG[F_M * cap + r] = g.m;
+    sG[F_H * cap + r] = g.h;
+  }
+  if (mask & 0x10u) {
+    sG[F_N * cap + r] = g.n;
+    sG[F_P * cap + r] = g.p;
+  }
+  if (mask & 0x20u) sG[F_XS * cap + r] = g.xs;
+  if (mask & 0x40u) {
+    sG[F_MA * cap + r] = g.ma;
+    sG[F_HA * cap + r] = g.ha;
+  }
+  if (mask & 0x80u) sG[F_XA * cap + r] = g.xa;
+}
+
 __device__ __forceinline__ unsigned long long pack_stamp(float v, unsigned stamp) {
   return ((unsigned long long)stamp << 32) | (unsigned long long)__float_as_uint(v);
 }
@@ -84,34 +139,38 @@ __device__ __forceinline__ unsigned long long pack_stamp(float v, unsigned stamp
 // Stamped exchange: copy words of slot `src` into dst (if not null) once their
 // stamp equals `want`.  Word i is src[lo + i], or src[list[i]] when list is
 // given.  Words of cells >= n_cells are never published and read as 0.
-// Each thread keeps up to four loads in flight; the wait is bounded by the
-// launch's timeout (error recorded, false returned).
+// Polling thread pt of T keeps kPollBatch loads in flight; the wait is bounded
+// by the launch's timeout (error recorded, false returned).
+constexpr int kPollBatch = 8;
 __device__ __forceinline__ bool poll_words(const StepArgs& a, const unsigned long long* src, int lo, int count,
-                                        const int* list, float* dst, unsigned want) {
-  const int T = blockDim.x;
+                                           const int* list, float* dst, unsigned want, int pt, int T) {
   uint64_t t0 = 0;
-  for (int base = threadIdx.x; base < count; base += 4 * T) {
-    unsigned long long w[4];
-    int cellid[4];
+  constexpr int B = kPollBatch;
+  for (int base = pt; base < count; base += B * T) {
+    unsigned long long w[B];
+    int cellid[B];
     unsigned pend = 0;
 #pragma unroll
-    for (int k = 0; k < 4; ++k) {
+    for (int k = 0; k < B; ++k) {
       const int i = base + k * T;
-      cellid[k] = -1;
+      cellid[k] = 0;
+      w[k] = 0;
       if (i < count) {
         const int c = list ? list[i] : lo + i;
         if (c < a.n_cells) {
           cellid[k] = c;
-          w[k] = ld_relaxed_gpu_u64(src + c);
           pend |= 1u << k;
         } else if (dst) {
           dst[i] = 0.0f;
         }
       }
     }
+#pragma unroll
+    for (int k = 0; k < B; ++k)
+      if ((pend >> k) & 1u) w[k] = ld_poll_u64(src + cellid[k]);
     while (true) {
 #pragma unroll
-      for (int k = 0; k < 4; ++k) {
+      for (int k = 0; k < B; ++k) {
         if (((pend >> k) & 1u) && (unsigned)(w[k] >> 32) == want) {
           if (dst) dst[base + k * T] = __uint_as_float((unsigned)w[k]);
           pend &= ~(1u << k);
@@ -126,8 +185,8 @@ __device__ __forceinline__ bool poll_words(const StepArgs& a, const unsigned lon
         return false;
       }
 #pragma unroll
-      for (int k = 0; k < 4; ++k)
-        if ((pend >> k) & 1u) w[k] = ld_relaxed_gpu_u64(src + cellid[k]);
+      for (int k = 0; k < B; ++k)
+        if ((pend >> k) & 1u) w[k] = ld_poll_u64(src + cellid[k]);
     }
   }
   return true;
@@ -234,11 +293,13 @@ __device__ __forceinline__ void couple_tile(const ChunkDesc* chunks, const uint1
   }
 }
 
-template <bool KAHAN, bool EDGE_G, bool LL>
-__global__ void __launch_bounds__(1024, 1) step_kernel(const __grid_constant__ StepArgs a) {
+// BLOCK threads per CTA, one CTA per SM: 1024 threads get 64 registers each,
+// 512 threads 128 (fewer warps, no spills).
+template <int BLOCK, bool KAHAN, bool EDGE_G, bool LL>
+__global__ void __launch_bounds__(BLOCK, 1) step_kernel(const __grid_constant__ StepArgs a) {
   extern __shared__ __align__(16) unsigned char smem_raw[];
   __shared__ int s_abort;
-  __shared__ unsigned long long s_prof[5];
+  __shared__ unsigned long long s_prof[6];
   const SmemShape shp = a.shape;
   const SmemLayout L = smem_layout(shp);
   float* tbuf = reinterpret_cast<float*>(smem_raw + L.tiles);
@@ -275,6 +336,17 @@ __global__ void __launch_bounds__(1024, 1) step_kernel(const __grid_constant__ S
   const bool unit_lane = unit_warp && ucell_l < w.n_cells;
   unsigned umask = 0;
   for (int u = warp % U; u < kUnits; u += U) umask |= 1u << u;
+  // stamped mode: threads from poll_first on gather the neighbours' words --
+  // the warps left over by the gate units when they can take every word in
+  // one batch of loads (they poll while the units compute), else every thread
+  // after its units
+  int poll_first = 0;
+  if (LL && ngroups * U < nwarps) {
+    int words = w.n_probes;
+    for (int j = 0; j < w.n_tiles; ++j) words += a.tiles[w.tile_begin + j].nfloats;
+    const int pollers = (int)blockDim.x - ngroups * U * 32;
+    if (pollers * kPollBatch >= words) poll_first = ngroups * U * 32;
+  }
 
   // ---- static work: either resident in shared memory or read from global.
   // Indices below are relative to the CTA's first chunk / edge.
@@ -346,27 +418,14 @@ __global__ void __launch_bounds__(1024, 1) step_kernel(const __grid_constant__ S
     s_abort = 0;
   }
 
-  // unit lanes hold the gate state of their cell in registers
-  Gates gs;
-  if (unit_lane) {
-    const int c = w.cell_begin + ucell_l;
+  // gate state of the owned cells lives in shared memory for the launch:
+  // field f of local cell r at sG[f * cap + r] (f = DevField), Ca2+ in sCa[r]
+  float* sG = reinterpret_cast<float*>(smem_raw + L.gates);
+  double* sCa = reinterpret_cast<double*>(smem_raw + L.gca);
+  if (owner) {
     const float* st = a.st;
-    gs.q = st[F_Q * np + c];
-    gs.r = st[F_R * np + c];
-    gs.s = st[F_S * np + c];
-    gs.Ca = a.ca[c];
-    gs.ICaH = st[F_ICAH * np + c];
-    gs.gCaL = st[F_GCAL * np + c];
-    gs.k = st[F_K * np + c];
-    gs.l = st[F_L * np + c];
-    gs.m = st[F_M * np + c];
-    gs.h = st[F_H * np + c];
-    gs.n = st[F_N * np + c];
-    gs.p = st[F_P * np + c];
-    gs.xs = st[F_XS * np + c];
-    gs.ma = st[F_MA * np + c];
-    gs.ha = st[F_HA * np + c];
-    gs.xa = st[F_XA * np + c];
+    for (int f = F_Q; f < F_COUNT; ++f) sG[f * cap + tid] = st[f * np + cell];
+    sCa[tid] = a.ca[cell];
   }
   // voltage threads hold the per-cell constants of the voltage step
   int2 slots = make_int2(0, 0);
@@ -385,11 +444,15 @@ __global__ void __launch_bounds__(1024, 1) step_kernel(const __grid_constant__ S
     }
     if (a.cell_step_off) my_off = a.cell_step_off[cell];
   }
+  const VoltCoef vk = volt_coef(a.P);
   const bool prof = a.prof != nullptr && tid == 0;
-  if (prof) s_prof[0] = s_prof[1] = s_prof[2] = s_prof[3] = s_prof[4] = 0;
+  if (prof) s_prof[0] = s_prof[1] = s_prof[2] = s_prof[3] = s_prof[4] = s_prof[5] = 0;
   __syncthreads();
 
-  uint64_t t_step = prof ? globaltimer_ns() : 0;
+  // phase timers count SM cycles; the launch's global-timer span calibrates them
+  const uint64_t ns_begin = prof ? globaltimer_ns() : 0;
+  const uint64_t cy_begin = prof ? clock64() : 0;
+  uint64_t t_step = cy_begin;
   unsigned nload = 0;  // bulk tile loads issued so far (same value in every thread)
   int row = 0;
   unsigned bar_target = 0;
@@ -416,7 +479,9 @@ __global__ void __launch_bounds__(1024, 1) step_kernel(const __grid_constant__ S
       v.Vs = sVs[ucell_l];
       v.Va = sVa[ucell_l];
       Currents cur;
+      Gates gs = load_gates(sG, sCa, cap, ucell_l, umask);
       run_units(a.P, umask, v, gs, cur);
+      store_gates(sG, sCa, cap, ucell_l, umask, gs);
       if (umask & 0x01u) sI[0 * cap + ucell_l] = cur.I_h;
       if (umask & 0x02u) {
         sI[1 * cap + ucell_l] = cur.I_CaH;
@@ -429,24 +494,31 @@ __global__ void __launch_bounds__(1024, 1) step_kernel(const __grid_constant__ S
       if (umask & 0x40u) sI[7 * cap + ucell_l] = cur.I_Na_a;
       if (umask & 0x80u) sI[8 * cap + ucell_l] = cur.I_K_a;
     }
+    const uint64_t t_units = prof ? clock64() : 0;
 
     // ---------------- phase A: gap-junction coupling
     if (LL) {
       // stamped exchange: gather every tile (and the progress probes) once
-      // the words carry this step's stamp, then reduce all chunks
-      const unsigned long long* src = a.vll[step & 1];
-      int toff = 0;
-      bool ok = true;
-      for (int j = 0; j < w.n_tiles && ok; ++j) {
-        const TileDesc td = tiles[j];
-        ok = poll_words(a, src, td.lo, td.nfloats, nullptr, tbuf + toff, (unsigned)step);
-        toff += td.nfloats;
+      // the words carry this step's stamp, then reduce all chunks.  The
+      // polling threads are the warps without gate units when there are any
+      // (they poll while the units compute), else every thread after its units.
+      if (tid >= poll_first) {
+        const unsigned long long* src = a.vll[step & 1];
+        const int pt = tid - poll_first, npt = blockDim.x - poll_first;
+        int toff = 0;
+        bool ok = true;
+        for (int j = 0; j < w.n_tiles && ok; ++j) {
+          const TileDesc td = tiles[j];
+          ok = poll_words(a, src, td.lo, td.nfloats, nullptr, tbuf + toff, (unsigned)step, pt, npt);
+          toff += td.nfloats;
+        }
+        if (ok && w.n_probes > 0)
+          ok = poll_words(a, src, 0, w.n_probes, a.probes + w.probe_begin, nullptr, (unsigned)step, pt, npt);
+        if (!ok) s_abort = 1;
       }
-      if (ok && w.n_probes > 0) ok = poll_words(a, src, 0, w.n_probes, a.probes + w.probe_begin, nullptr, (unsigned)step);
-      if (!ok) s_abort = 1;
       __syncthreads();
       if (s_abort) break;
-      if (prof) t_ready = globaltimer_ns();
+      if (prof) t_ready = clock64();
       couple_packed<KAHAN, EDGE_G>(smem_raw, L, w.n_groups, sVd, part, partc, warp, nwarps, lane);
       __syncthreads();
     } else if (w.n_tiles > 0) {
@@ -465,17 +537,17 @@ __global__ void __launch_bounds__(1024, 1) step_kernel(const __grid_constant__ S
           issue_tile(a, vcur, tiles[j + 1], tbuf + b1 * tile_cap, &mbar[b1]);
         }
         if (!wait_tile(a, &mbar[b], (k / (unsigned)nbuf) & 1u)) s_abort = 1;
-        if (prof && j == 0) t_ready = globaltimer_ns();
+        if (prof && j == 0) t_ready = clock64();
         couple_tile<KAHAN, EDGE_G>(chunks, edges, edge_g, td.chunk_begin - chunk0, td.chunk_end - chunk0, edge0,
                                    buf, sVd, part, partc, warp, nwarps, lane);
         __syncthreads();
       }
       nload += w.n_tiles;
     } else {
-      if (prof) t_ready = globaltimer_ns();
+      if (prof) t_ready = clock64();
       __syncthreads();
     }
-    const uint64_t t_coupled = prof ? globaltimer_ns() : 0;
+    const uint64_t t_coupled = prof ? clock64() : 0;
 
     // ---------------- phase B: voltage step, one thread per owned cell
     if (owner) {
@@ -490,8 +562,18 @@ __global__ void __launch_bounds__(1024, 1) step_kernel(const __grid_constant__ S
         }
         ic = s;
       } else {
+        // in slot (= sender) order; four loads in flight at a time
         ic = 0.0f;
-        for (int q = 0; q < slots.y; ++q) ic += part[slots.x + q];
+        const float* ps = part + slots.x;
+        int q = 0;
+        for (; q + 4 <= slots.y; q += 4) {
+          const float p0 = ps[q], p1 = ps[q + 1], p2 = ps[q + 2], p3 = ps[q + 3];
+          ic += p0;
+          ic += p1;
+          ic += p2;
+          ic += p3;
+        }
+        for (; q < slots.y; ++q) ic += ps[q];
       }
       if (!EDGE_G) ic *= gscale;
       const int ls = step + my_off;
@@ -516,7 +598,7 @@ __global__ void __launch_bounds__(1024, 1) step_kernel(const __grid_constant__ S
       v.Vd = sVd[tid];
       v.Vs = sVs[tid];
       v.Va = sVa[tid];
-      voltage_step(a.P, v, cur, ic, iapp);
+      voltage_step(a.P, vk, v, cur, ic, iapp);
       if (LL)
         st_relaxed_gpu_u64(a.vll[(step + 1) & 1] + cell, pack_stamp(v.Vd, (unsigned)(step + 1)));
       else
@@ -535,11 +617,12 @@ __global__ void __launch_bounds__(1024, 1) step_kernel(const __grid_constant__ S
     if (a.trace_every > 0 && (step % a.trace_every) == 0) ++row;
 
     if (LL) {
-      uint64_t t_arrive = prof ? globaltimer_ns() : 0;
+      uint64_t t_arrive = prof ? clock64() : 0;
       __syncthreads();  // new voltages / free tile buffers before the next step
       if (prof) {
-        const uint64_t t_done = globaltimer_ns();
-        s_prof[0] += t_ready - t_step;
+        const uint64_t t_done = clock64();
+        s_prof[0] += t_ready - t_units;
+        s_prof[5] += t_units - t_step;
         s_prof[1] += t_coupled - t_ready;
         s_prof[2] += t_arrive - t_coupled;
         s_prof[3] += t_done - t_arrive;
@@ -551,8 +634,9 @@ __global__ void __launch_bounds__(1024, 1) step_kernel(const __grid_constant__ S
       uint64_t t_arrive = 0;
       const bool ok = grid_sync(a, bar_target, &s_abort, prof ? &t_arrive : nullptr);
       if (prof) {
-        const uint64_t t_done = globaltimer_ns();
-        s_prof[0] += t_ready - t_step;
+        const uint64_t t_done = clock64();
+        s_prof[0] += t_ready - t_units;
+        s_prof[5] += t_units - t_step;
         s_prof[1] += t_coupled - t_ready;
         s_prof[2] += t_arrive - t_coupled;
         s_prof[3] += t_done - t_arrive;
@@ -569,52 +653,44 @@ __global__ void __launch_bounds__(1024, 1) step_kernel(const __grid_constant__ S
     atomicAdd(pr + PROF_UPDATE, s_prof[2]);
     atomicAdd(pr + PROF_BARRIER, s_prof[3]);
     atomicAdd(pr + PROF_STEPS, s_prof[4]);
+    atomicAdd(pr + PROF_UNITS, s_prof[5]);
+    atomicAdd(pr + PROF_SPAN_NS, (unsigned long long)(globaltimer_ns() - ns_begin));
+    atomicAdd(pr + PROF_SPAN_CYCLES, (unsigned long long)(clock64() - cy_begin));
   }
   __syncthreads();
 
-  if (unit_lane) {
-    const int c = w.cell_begin + ucell_l;
-    float* st = a.st;
-    if (umask & 0x01u) st[F_Q * np + c] = gs.q;
-    if (umask & 0x02u) {
-      st[F_R * np + c] = gs.r;
-      st[F_S * np + c] = gs.s;
-      a.ca[c] = gs.Ca;
-      st[F_ICAH * np + c] = gs.ICaH;
-    }
-    if (umask & 0x04u) {
-      st[F_K * np + c] = gs.k;
-      st[F_L * np + c] = gs.l;
-    }
-    if (umask & 0x08u) {
-      st[F_M * np + c] = gs.m;
-      st[F_H * np + c] = gs.h;
-    }
-    if (umask & 0x10u) {
-      st[F_N * np + c] = gs.n;
-      st[F_P * np + c] = gs.p;
-    }
-    if (umask & 0x20u) st[F_XS * np + c] = gs.xs;
-    if (umask & 0x40u) {
-      st[F_MA * np + c] = gs.ma;
-      st[F_HA * np + c] = gs.ha;
-    }
-    if (umask & 0x80u) st[F_XA * np + c] = gs.xa;
-  }
   if (owner) {
+    float* st = a.st;
+    for (int f = F_Q; f < F_COUNT; ++f) st[f * np + cell] = sG[f * cap + tid];
+    a.ca[cell] = sCa[tid];
     if (LL) a.vd[(a.step0 + a.n_steps) & 1][cell] = sVd[tid];
-    a.st[F_VS * np + cell] = sVs[tid];
-    a.st[F_VA * np + cell] = sVa[tid];
+    st[F_VS * np + cell] = sVs[tid];
+    st[F_VA * np + cell] = sVa[tid];
   }
 }
 
-template <bool K, bool G, bool LL>
-cudaError_t launch_variant(const StepArgs& a, int grid, int threads, size_t smem, cudaStream_t stream) {
-  auto fn = step_kernel<K, G, LL>;
+template <int BLOCK, bool K, bool G, bool LL>
+cudaError_t launch_variant(const StepArgs& a, int grid, size_t smem, cudaStream_t stream) {
+  auto fn = step_kernel<BLOCK, K, G, LL>;
   cudaError_t e = cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
   if (e != cudaSuccess) return e;
   void* args[] = {const_cast<StepArgs*>(&a)};
-  return cudaLaunchCooperativeKernel((const void*)fn, dim3(grid), dim3(threads), args, smem, stream);
+  return cudaLaunchCooperativeKernel((const void*)fn, dim3(grid), dim3(BLOCK), args, smem, stream);
+}
+
+template <int BLOCK>
+cudaError_t launch_block(const StepArgs& a, int grid, size_t smem, cudaStream_t stream) {
+  const bool g = a.edge_g != nullptr;
+  if (a.shape.stamped) {
+    if (a.shape.kahan) return g ? launch_variant<BLOCK, true, true, true>(a, grid, smem, stream)
+                                : launch_variant<BLOCK, true, false, true>(a, grid, smem, stream);
+    return g ? launch_variant<BLOCK, false, true, true>(a, grid, smem, stream)
+             : launch_variant<BLOCK, false, false, true>(a, grid, smem, stream);
+  }
+  if (a.shape.kahan) return g ? launch_variant<BLOCK, true, true, false>(a, grid, smem, stream)
+                              : launch_variant<BLOCK, true, false, false>(a, grid, smem, stream);
+  return g ? launch_variant<BLOCK, false, true, false>(a, grid, smem, stream)
+           : launch_variant<BLOCK, false, false, false>(a, grid, smem, stream);
 }
 
 }  // namespace
@@ -623,27 +699,29 @@ size_t step_kernel_smem(const StepArgs& a) { return smem_layout(a.shape).total; 
 
 cudaError_t launch_step_kernel(const StepArgs& a, int grid, int threads, cudaStream_t stream) {
   const size_t smem = step_kernel_smem(a);
-  const bool g = a.edge_g != nullptr;
   if (threads != a.shape.threads) return cudaErrorInvalidValue;
-  if (a.shape.stamped) {
-    if (a.shape.kahan) return g ? launch_variant<true, true, true>(a, grid, threads, smem, stream)
-                                : launch_variant<true, false, true>(a, grid, threads, smem, stream);
-    return g ? launch_variant<false, true, true>(a, grid, threads, smem, stream)
-             : launch_variant<false, false, true>(a, grid, threads, smem, stream);
-  }
-  if (a.shape.kahan) return g ? launch_variant<true, true, false>(a, grid, threads, smem, stream)
-                              : launch_variant<true, false, false>(a, grid, threads, smem, stream);
-  return g ? launch_variant<false, true, false>(a, grid, threads, smem, stream)
-           : launch_variant<false, false, false>(a, grid, threads, smem, stream);
+  if (threads == 1024) return launch_block<1024>(a, grid, smem, stream);
+  if (threads == 512) return launch_block<512>(a, grid, smem, stream);
+  return cudaErrorInvalidValue;
 }
 
 int max_coresident_ctas(int threads, size_t smem) {
   int dev = 0, nsm = 0, per_sm = 0;
   cudaGetDevice(&dev);
   cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev);
-  auto fn = step_kernel<false, false, false>;
-  cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-  if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, fn, threads, smem) != cudaSuccess) return 0;
+  cudaError_t e;
+  if (threads == 1024) {
+    auto fn = step_kernel<1024, false, false, false>;
+    cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, fn, threads, smem);
+  } else if (threads == 512) {
+    auto fn = step_kernel<512, false, false, false>;
+    cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, fn, threads, smem);
+  } else {
+    return 0;
+  }
+  if (e != cudaSuccess) return 0;
   return per_sm * nsm;
 }
 

@@ -73,9 +73,14 @@ struct StepArgs {
   unsigned long long* prof;
 };
 
-// Phase timer slots written when StepArgs::prof is set: staging wait,
-// coupling, update (incl. CTA stragglers), grid barrier, steps counted.
-enum { PROF_STAGE = 0, PROF_COUPLE, PROF_UPDATE, PROF_BARRIER, PROF_STEPS, kProfSlots = 8 };
+// Phase timer slots written when StepArgs::prof is set, in SM cycles: staging
+// wait (after the gate units), coupling, update (incl. CTA stragglers), grid
+// barrier, steps counted, gate units; and the launch's span in global-timer ns
+// and in SM cycles, which converts the others to time.
+enum {
+  PROF_STAGE = 0, PROF_COUPLE, PROF_UPDATE, PROF_BARRIER, PROF_STEPS, PROF_UNITS, PROF_SPAN_NS,
+  PROF_SPAN_CYCLES, kProfSlots = 8
+};
 
 // Dynamic shared memory needed for a launch.
 size_t step_kernel_smem(const StepArgs& a);

@@ -100,15 +100,19 @@ typedef struct {
 // Number of per-cell float arrays kept in shared memory: V_dend, V_soma,
 // V_axon and the nine gate-unit currents.
 enum { kCellArrays = 12 };
+// Per-cell gate state in shared memory: 17 float fields (indexed like the
+// device state arrays) plus the FP64 Ca2+ concentration.
+enum { kGateFloats = 17 };
 
 // Dynamic shared-memory layout of the step kernel (byte offsets):
 //   [tile buffers: nbuf x tile_cap floats]
 //   [cell arrays: kCellArrays x cells_cap floats]
+//   [gate state: cells_cap doubles (Ca2+), kGateFloats x cells_cap floats]
 //   [partial sums: max_slots floats][Kahan compensations: max_slots floats]
 //   [2 mbarriers, 16-byte aligned]
 //   resident plans only: [tile descs][chunk descs][per-edge g][edge offsets]
 typedef struct {
-  size_t tiles, vown, part, partc, mbar, tdesc, chunks, eg, edges, total;
+  size_t tiles, vown, gates, gca, part, partc, mbar, tdesc, chunks, eg, edges, total;
 } SmemLayout;
 
 static inline INFOLI_HD SmemLayout smem_layout(SmemShape s) {
@@ -118,6 +122,11 @@ static inline INFOLI_HD SmemLayout smem_layout(SmemShape s) {
   off += (size_t)s.nbuf * (size_t)s.tile_cap * sizeof(float);
   L.vown = off;
   off += (size_t)kCellArrays * (size_t)s.cells_cap * sizeof(float);
+  off = (off + 7) & ~(size_t)7;
+  L.gca = off;
+  off += (size_t)s.cells_cap * sizeof(double);
+  L.gates = off;
+  off += (size_t)kGateFloats * (size_t)s.cells_cap * sizeof(float);
   L.part = off;
   off += (size_t)s.max_slots * sizeof(float);
   L.partc = off;

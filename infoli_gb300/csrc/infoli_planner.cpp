@@ -164,24 +164,75 @@ void pack_groups(Plan& P, const SmemLayout& L, const PlanInput& in, const std::v
         pad[l] = (uint16_t)(L.vown + sizeof(float) * (size_t)d.y);
         gdesc.push_back(d);
       }
-      // greedy bank-distinct dealing, position by position
+      // bank-distinct dealing, position by position: lanes whose chunk is
+      // exhausted read their padding word (lanes of one receiver share it);
+      // the others are matched to free banks by augmenting paths (Kuhn), so
+      // each position has as many conflict-free lanes as the remaining
+      // entries allow; unmatched lanes take any entry
       std::vector<std::pair<uint16_t, float>> cell(32 * kLaneEdges);
       for (int k = 0; k < kLaneEdges; ++k) {
-        unsigned used = 0;
-        for (int l = 0; l < 32; ++l) {
-          std::pair<uint16_t, float> pick = {pad[l], 0.0f};
-          if (!rem[l].empty()) {
-            size_t best = rem[l].size() - 1;
-            for (size_t q = 0; q < rem[l].size(); ++q)
-              if (!((used >> ((rem[l][q].first >> 2) & 31)) & 1u)) {
-                best = q;
-                break;
-              }
-            pick = rem[l][best];
-            rem[l].erase(rem[l].begin() + best);
+        int bank_word[32];
+        for (int b2 = 0; b2 < 32; ++b2) bank_word[b2] = -1;
+        for (int l = 0; l < 32; ++l)
+          if (rem[l].empty()) {
+            cell[l * kLaneEdges + k] = {pad[l], 0.0f};
+            const int wd = pad[l] >> 2;
+            if (bank_word[wd & 31] < 0) bank_word[wd & 31] = wd;
           }
-          used |= 1u << ((pick.first >> 2) & 31);
-          cell[l * kLaneEdges + k] = pick;
+        unsigned adj[32];
+        for (int l = 0; l < 32; ++l) {
+          adj[l] = 0;
+          for (const auto& e : rem[l]) {
+            const int b2 = (e.first >> 2) & 31;
+            if (bank_word[b2] < 0) adj[l] |= 1u << b2;
+          }
+        }
+        int match_bank[32];  // bank -> lane
+        for (int b2 = 0; b2 < 32; ++b2) match_bank[b2] = -1;
+        for (int l = 0; l < 32; ++l) {
+          if (!adj[l]) continue;
+          unsigned seen = 0;
+          // iterative augmenting-path search from lane l
+          struct Frame {
+            int lane;
+            unsigned left;
+          };
+          Frame stack[33];
+          int prev_bank[33];
+          int sp = 0;
+          stack[0] = {l, adj[l]};
+          bool done = false;
+          while (sp >= 0 && !done) {
+            Frame& f = stack[sp];
+            const unsigned cand = f.left & ~seen;
+            if (!cand) {
+              --sp;
+              continue;
+            }
+            const int b2 = __builtin_ctz(cand);
+            f.left &= ~(1u << b2);
+            seen |= 1u << b2;
+            prev_bank[sp] = b2;
+            if (match_bank[b2] < 0) {
+              for (int q = sp; q >= 0; --q) match_bank[prev_bank[q]] = stack[q].lane;
+              done = true;
+            } else if (sp + 1 < 33) {
+              ++sp;
+              stack[sp] = {match_bank[b2], adj[match_bank[b2]]};
+            }
+          }
+        }
+        int lane_bank[32];
+        for (int l = 0; l < 32; ++l) lane_bank[l] = -1;
+        for (int b2 = 0; b2 < 32; ++b2)
+          if (match_bank[b2] >= 0) lane_bank[match_bank[b2]] = b2;
+        for (int l = 0; l < 32; ++l) {
+          if (rem[l].empty()) continue;
+          size_t q = 0;
+          if (lane_bank[l] >= 0)
+            while (((rem[l][q].first >> 2) & 31) != lane_bank[l]) ++q;
+          cell[l * kLaneEdges + k] = rem[l][q];
+          rem[l].erase(rem[l].begin() + q);
         }
       }
       // transposed quads: ((g * kQuads + k / 4) * 32 + l) * 4 + k % 4
@@ -502,7 +553,7 @@ bool make_plan(const PlanInput& in, Plan* out, std::string* err) {
 // CPU test suite to validate the planner without a GPU.
 extern "C" int infoli_plan_emulate(int n, const int64_t* row_ptr, const int32_t* col, const float* g,
                                    float g_uniform, int grid, int grid_max, int threads, int64_t smem_budget,
-                                   int sync_mode, const float* vdend, float* ic_out, int64_t info[8]) {
+                                   int sync_mode, const float* vdend, float* ic_out, int64_t info[10]) {
   using namespace infoli;
   PlanInput in;
   in.n = n;
@@ -521,7 +572,7 @@ extern "C" int infoli_plan_emulate(int n, const int64_t* row_ptr, const int32_t*
   if (L.total > (size_t)smem_budget) return -2;
   auto fexp = [](float V) { return 0.8f * std::exp(-(V * V) / 100.0f) + 0.2f; };
   std::vector<unsigned char> sm(L.total);
-  int64_t groups = 0, probes = 0;
+  int64_t groups = 0, probes = 0, gather_waves = 0, gathers = 0;
   for (const CtaWork& w : P.cta) {
     if (w.n_cells > threads || w.n_cells > P.shape.cells_cap) return -3;
     std::fill(sm.begin(), sm.end(), 0);
@@ -541,6 +592,24 @@ extern "C" int infoli_plan_emulate(int n, const int64_t* row_ptr, const int32_t*
         if (P.probes[w.probe_begin + q] < 0 || P.probes[w.probe_begin + q] >= n) return -5;
       probes += w.n_probes;
       groups += w.n_groups;
+      // shared-memory wavefronts of the V_dend gathers: per (group, entry
+      // position) the largest number of distinct words any bank serves
+      for (int gi = 0; gi < w.n_groups; ++gi)
+        for (int k = 0; k < kLaneEdges; ++k) {
+          unsigned words[32][32];
+          int cnt[32] = {0};
+          int worst = 1;
+          for (int l = 0; l < 32; ++l) {
+            const size_t at = (((size_t)w.group_begin + gi) * kQuads + k / 4) * 32 * 4 + (size_t)l * 4 + k % 4;
+            const unsigned word = P.edges[at] >> 2, bank = word & 31;
+            bool seen = false;
+            for (int q = 0; q < cnt[bank]; ++q) seen |= words[bank][q] == word;
+            if (!seen) words[bank][cnt[bank]++] = word;
+            worst = std::max(worst, cnt[bank]);
+          }
+          gather_waves += worst;
+          gathers += 1;
+        }
       for (int gi = 0; gi < w.n_groups; ++gi)
         for (int l = 0; l < 32; ++l) {
           const int2_t d = P.gdesc[((size_t)w.group_begin + gi) * 32 + l];
@@ -592,6 +661,8 @@ extern "C" int infoli_plan_emulate(int n, const int64_t* row_ptr, const int32_t*
     info[5] = (int64_t)P.smem_bytes;
     info[6] = probes;
     info[7] = P.shape.res_chunks > 0;
+    info[8] = gather_waves;
+    info[9] = gathers;
   }
   return 0;
 }

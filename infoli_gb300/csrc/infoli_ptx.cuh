@@ -32,6 +32,13 @@ __device__ __forceinline__ unsigned long long ld_relaxed_gpu_u64(const unsigned 
   asm volatile("ld.relaxed.gpu.global.u64 %0, [%1];" : "=l"(v) : "l"(p) : "memory");
   return v;
 }
+// Same load for polling loops: no "memory" clobber, so independent polls may
+// be issued back to back (each still re-reads memory: the asm is volatile).
+__device__ __forceinline__ unsigned long long ld_poll_u64(const unsigned long long* p) {
+  unsigned long long v;
+  asm volatile("ld.relaxed.gpu.global.u64 %0, [%1];" : "=l"(v) : "l"(p));
+  return v;
+}
 __device__ __forceinline__ void st_relaxed_gpu_u64(unsigned long long* p, unsigned long long v) {
   asm volatile("st.relaxed.gpu.global.u64 [%0], %1;" ::"l"(p), "l"(v) : "memory");
 }
