@@ -213,6 +213,40 @@ int infoli_sim_get_profile(infoli_sim* s, double mean_ns[5], double max_ns[5]);
 
 int infoli_sim_destroy(infoli_sim* s);
 
+/* ------------------------------------------------------------------------ */
+/* allocation-free run                                                       */
+/* ------------------------------------------------------------------------ */
+
+/* No counterpart in the reference (its simulator allocates all of its own
+ * memory).  For callers that must not allocate device memory while they run
+ * the network -- code executing during CUDA stream capture, where cudaMalloc
+ * is not allowed, or hosts and language bindings that own every device
+ * buffer and hand the library only their own -- this runs n_steps steps
+ * without allocating anything: no cudaMalloc / cudaFree, no allocating
+ * library call.  Everything is passed in device memory by the caller:
+ *   d_row_ptr[n+1], d_col[E], d_g[E] or NULL (then g_uniform on every edge):
+ *       CSR topology by receiver;
+ *   d_state[INFOLI_NSTATE * n]: the 19 state arrays (SoA, bin/default.conf
+ *       order), read at the start and overwritten with the state after the
+ *       run;
+ *   d_trace_axon[n_steps * n] or NULL: V_axon after every step.
+ * The stimulus is one global pulse (pulse_amp for pulse_start <= step <
+ * pulse_end; the reference's default is 20000, 20499, 6).  step0 is the index
+ * of the first step.  `stream` is a cudaStream_t (NULL: the default stream);
+ * the call returns after the run has finished on it.
+ * The only scratch (V_dend double buffer, barrier counter, error word) is a
+ * static device array of fixed size in the library, so networks are limited
+ * to 65536 cells (INFOLI_ERR_CAPACITY beyond).  Every GPU that loads the
+ * library holds that array (about 0.5 MiB) until the process exits.  The
+ * first call on a device looks up the array's device address (with that
+ * device current): make that first call before any stream capture.  All
+ * calls share the array, so calls that overlap on the GPU (different
+ * streams, threads or processes sharing a context) race and must be
+ * serialised by the caller. */
+int infoli_run_noalloc(const float* params, int n_cells, const int64_t* d_row_ptr, const int32_t* d_col,
+                       const float* d_g, float g_uniform, int pulse_start, int pulse_end, float pulse_amp,
+                       float* d_state, int step0, int n_steps, float* d_trace_axon, void* stream);
+
 /* Host-side check of the work planner (no GPU needed; no counterpart in the
  * reference): plans an n-cell network for a device with grid_max co-resident
  * CTAs of `threads` threads and smem_budget bytes of shared memory per CTA

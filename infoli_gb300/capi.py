@@ -41,6 +41,7 @@ EXPORTED = [
     "infoli_sim_run_into", "infoli_sim_get_state", "infoli_sim_set_state", "infoli_sim_step",
     "infoli_sim_last_run_stats", "infoli_sim_plan_info", "infoli_sim_destroy", "infoli_format_f8",
     "infoli_format_row", "infoli_sim_set_profiling", "infoli_sim_get_profile", "infoli_plan_emulate",
+    "infoli_run_noalloc",
 ]
 
 
@@ -102,6 +103,7 @@ def load():
         "infoli_sim_plan_info": ([P, P, P, P, P, P], I),
         "infoli_sim_destroy": ([P], I),
         "infoli_plan_emulate": ([I, P, P, P, F, I, I, I, I64, I, P, P, P], I),
+        "infoli_run_noalloc": ([P, I, P, P, P, F, I, I, F, P, I, I, P, P], I),
         "infoli_sim_set_profiling": ([P, I], I),
         "infoli_sim_get_profile": ([P, P, P], I),
         "infoli_format_f8": ([C.c_char_p, F], I),
