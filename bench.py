@@ -36,6 +36,19 @@ STEPS_PER_ITER = 1000
 TRACE_EVERY = 100
 
 
+def ncu_traffic():
+    """DRAM bytes (read + write) of one step-kernel launch of this workload, from
+    the committed ncu summary (profiles/step_kernel_grid10k_stamped.md)."""
+    import re
+
+    try:
+        with open(os.path.join(ROOT, "profiles", "step_kernel_grid10k_stamped.md")) as f:
+            m = re.search(r"traffic \(read \+ write\) per launch \| ([\d,]+) B", f.read())
+        return int(m.group(1).replace(",", "")) if m else None
+    except OSError:
+        return None
+
+
 def peaks():
     try:
         with open(os.path.join(ROOT, "MEASURED_PEAKS.json")) as f:
@@ -285,9 +298,12 @@ def run_gpu(args, world, rank, local):
             "gpu_launches": launches,
             "wall_s": wall,
             "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
-                         "frac": achieved / peak, "traffic": None,
-                         "note": f"algorithmic bytes (132 + N/8) per cell-step over the step kernel's mean "
-                                 f"launch time; peak {peak_kind}"},
+                         "frac": achieved / peak, "traffic": ncu_traffic(),
+                         "note": f"achieved = algorithmic bytes (132 + N/8 per cell-step) x cells x "
+                                 f"{STEPS_PER_ITER} timesteps over the step kernel's mean launch time "
+                                 f"(CUDA events); peak {peak_kind} HBM copy bandwidth; traffic = ncu "
+                                 f"DRAM read+write of one launch of this workload (profiles/): the "
+                                 f"topology and V_dend windows stay on chip, the step is latency-bound"},
             "phase_ns_per_timestep": prof["max"],
             "clocks": clocks,
             "cpu_baseline": {"value": cpu_rate, "unit": "cell-steps/s", "cores": threads, "kind": "port",
