@@ -136,60 +136,103 @@ __device__ __forceinline__ unsigned long long pack_stamp(float v, unsigned stamp
   return ((unsigned long long)stamp << 32) | (unsigned long long)__float_as_uint(v);
 }
 
-// Stamped exchange: copy words of slot `src` into dst (if not null) once their
-// stamp equals `want`.  Word i is src[lo + i], or src[list[i]] when list is
-// given.  Words of cells >= n_cells are never published and read as 0.
-// Polling thread pt of T keeps kPollBatch loads in flight; the wait is bounded
-// by the launch's timeout (error recorded, false returned).
+// Stamped exchange.  A CTA's window is one flat index space: word i <
+// tile_words is word i of its tiles laid end to end (as they sit in shared
+// memory), word i >= tile_words is progress probe i - tile_words (checked,
+// not stored).  Words of cells >= n_cells are never published and read as 0.
+// Polling thread pt of T takes words pt, pt + T, ... in batches of
+// kPollBatch loads in flight.  A batch can be issued early and finished later
+// (the loads overlap other work); every wait is bounded by the launch's
+// timeout (error recorded, false returned).
 constexpr int kPollBatch = 8;
-__device__ __forceinline__ bool poll_words(const StepArgs& a, const unsigned long long* src, int lo, int count,
-                                           const int* list, float* dst, unsigned want, int pt, int T) {
-  uint64_t t0 = 0;
-  constexpr int B = kPollBatch;
-  for (int base = pt; base < count; base += B * T) {
-    unsigned long long w[B];
-    int cellid[B];
-    unsigned pend = 0;
-#pragma unroll
-    for (int k = 0; k < B; ++k) {
-      const int i = base + k * T;
-      cellid[k] = 0;
-      w[k] = 0;
-      if (i < count) {
-        const int c = list ? list[i] : lo + i;
-        if (c < a.n_cells) {
-          cellid[k] = c;
-          pend |= 1u << k;
-        } else if (dst) {
-          dst[i] = 0.0f;
-        }
-      }
+
+struct PollWindow {
+  const TileDesc* tiles;
+  int n_tiles;
+  const int* probes;
+  int n_probes;
+  int tile_words;
+  int total;
+};
+
+struct PollBatch {
+  unsigned long long w[kPollBatch];
+  int cell[kPollBatch];
+  int dst[kPollBatch];  // shared-memory word, or -1 for a probe
+  unsigned pend;
+};
+
+__device__ __forceinline__ int window_cell(const PollWindow& pw, int i, int* dst) {
+  if (i >= pw.tile_words) {
+    *dst = -1;
+    return pw.probes[i - pw.tile_words];
+  }
+  int toff = 0;
+  for (int j = 0; j < pw.n_tiles; ++j) {
+    const int nf = pw.tiles[j].nfloats;
+    if (i < toff + nf) {
+      *dst = i;
+      return pw.tiles[j].lo + (i - toff);
     }
+    toff += nf;
+  }
+  *dst = -1;
+  return 0;
+}
+
+// tbuf receives each word at its window index and, when dup > 0, again at
+// dup + index (the bank-shifted second copy).
+__device__ __forceinline__ void poll_issue(const StepArgs& a, const unsigned long long* src, const PollWindow& pw,
+                                           int base, int T, float* tbuf, int dup, PollBatch& b) {
+  b.pend = 0;
 #pragma unroll
-    for (int k = 0; k < B; ++k)
-      if ((pend >> k) & 1u) w[k] = ld_poll_u64(src + cellid[k]);
-    while (true) {
-#pragma unroll
-      for (int k = 0; k < B; ++k) {
-        if (((pend >> k) & 1u) && (unsigned)(w[k] >> 32) == want) {
-          if (dst) dst[base + k * T] = __uint_as_float((unsigned)w[k]);
-          pend &= ~(1u << k);
-        }
+  for (int k = 0; k < kPollBatch; ++k) {
+    const int i = base + k * T;
+    b.cell[k] = 0;
+    b.dst[k] = -1;
+    b.w[k] = 0;
+    if (i < pw.total) {
+      const int c = window_cell(pw, i, &b.dst[k]);
+      if (c < a.n_cells) {
+        b.cell[k] = c;
+        b.pend |= 1u << k;
+      } else if (b.dst[k] >= 0) {
+        tbuf[b.dst[k]] = 0.0f;
+        if (dup) tbuf[dup + b.dst[k]] = 0.0f;
       }
-      if (!pend) break;
-      const uint64_t now = globaltimer_ns();
-      if (t0 == 0) {
-        t0 = now;
-      } else if (now - t0 > a.timeout_ns || ld_relaxed_gpu(a.err) != 0) {
-        atomicCAS(a.err, 0, DEV_ERR_STAMP_TIMEOUT);
-        return false;
-      }
-#pragma unroll
-      for (int k = 0; k < B; ++k)
-        if ((pend >> k) & 1u) w[k] = ld_poll_u64(src + cellid[k]);
     }
   }
-  return true;
+#pragma unroll
+  for (int k = 0; k < kPollBatch; ++k)
+    if ((b.pend >> k) & 1u) b.w[k] = ld_poll_u64(src + b.cell[k]);
+}
+
+__device__ __forceinline__ bool poll_finish(const StepArgs& a, const unsigned long long* src, float* tbuf, int dup,
+                                            unsigned want, PollBatch& b, uint64_t& t0) {
+  while (true) {
+#pragma unroll
+    for (int k = 0; k < kPollBatch; ++k) {
+      if (((b.pend >> k) & 1u) && (unsigned)(b.w[k] >> 32) == want) {
+        if (b.dst[k] >= 0) {
+          const float v = __uint_as_float((unsigned)b.w[k]);
+          tbuf[b.dst[k]] = v;
+          if (dup) tbuf[dup + b.dst[k]] = v;
+        }
+        b.pend &= ~(1u << k);
+      }
+    }
+    if (!b.pend) return true;
+    const uint64_t now = globaltimer_ns();
+    if (t0 == 0) {
+      t0 = now;
+    } else if (now - t0 > a.timeout_ns || ld_relaxed_gpu(a.err) != 0) {
+      atomicCAS(a.err, 0, DEV_ERR_STAMP_TIMEOUT);
+      return false;
+    }
+#pragma unroll
+    for (int k = 0; k < kPollBatch; ++k)
+      if ((b.pend >> k) & 1u) b.w[k] = ld_poll_u64(src + b.cell[k]);
+  }
 }
 
 // Phase A of stamped plans (packed lane-chunk layout, all in shared memory):
@@ -210,7 +253,7 @@ __device__ __forceinline__ void couple_packed(const unsigned char* sm, const Sme
     const int2 d = gd[gi * 32 + lane];  // {slot, recv}
     const float vc = sVd[d.y];
     float acc0 = 0.0f, acc1 = 0.0f, cmp0 = 0.0f, cmp1 = 0.0f;
-#pragma unroll 2
+#pragma unroll
     for (int kq = 0; kq < kQuads; ++kq) {
       const int qi = (gi * kQuads + kq) * 32 + lane;
       const uint2 o = ent[qi];
@@ -340,13 +383,19 @@ __global__ void __launch_bounds__(BLOCK, 1) step_kernel(const __grid_constant__ 
   // the warps left over by the gate units when they can take every word in
   // one batch of loads (they poll while the units compute), else every thread
   // after its units
+  PollWindow pw{};
   int poll_first = 0;
-  if (LL && ngroups * U < nwarps) {
-    int words = w.n_probes;
-    for (int j = 0; j < w.n_tiles; ++j) words += a.tiles[w.tile_begin + j].nfloats;
+  if (LL) {
+    pw.n_tiles = w.n_tiles;
+    pw.probes = a.probes + w.probe_begin;
+    pw.n_probes = w.n_probes;
+    for (int j = 0; j < w.n_tiles; ++j) pw.tile_words += a.tiles[w.tile_begin + j].nfloats;
+    pw.total = pw.tile_words + pw.n_probes;
     const int pollers = (int)blockDim.x - ngroups * U * 32;
-    if (pollers * kPollBatch >= words) poll_first = ngroups * U * 32;
+    if (ngroups * U < nwarps && pollers * kPollBatch >= pw.total) poll_first = ngroups * U * 32;
   }
+  // (Issuing the first poll batch before the gate units was measured slower:
+  // the outstanding loads delay the units' shared-memory traffic.)
 
   // ---- static work: either resident in shared memory or read from global.
   // Indices below are relative to the CTA's first chunk / edge.
@@ -372,6 +421,7 @@ __global__ void __launch_bounds__(BLOCK, 1) step_kernel(const __grid_constant__ 
       for (int i = tid; i < nq; i += blockDim.x) s_g[i] = gg[i];
     }
     tiles = s_t;
+    pw.tiles = s_t;
   } else if (w.n_tiles > 0) {
     chunk0 = tiles[0].chunk_begin;
     const int chunk1 = tiles[w.n_tiles - 1].chunk_end;
@@ -503,17 +553,15 @@ __global__ void __launch_bounds__(BLOCK, 1) step_kernel(const __grid_constant__ 
       // polling threads are the warps without gate units when there are any
       // (they poll while the units compute), else every thread after its units.
       if (tid >= poll_first) {
-        const unsigned long long* src = a.vll[step & 1];
+        const unsigned long long* vsrc = a.vll[step & 1];
         const int pt = tid - poll_first, npt = blockDim.x - poll_first;
-        int toff = 0;
+        uint64_t pt0 = 0;
         bool ok = true;
-        for (int j = 0; j < w.n_tiles && ok; ++j) {
-          const TileDesc td = tiles[j];
-          ok = poll_words(a, src, td.lo, td.nfloats, nullptr, tbuf + toff, (unsigned)step, pt, npt);
-          toff += td.nfloats;
+        PollBatch pb;
+        for (int base = pt; ok && base < pw.total; base += kPollBatch * npt) {
+          poll_issue(a, vsrc, pw, base, npt, tbuf, shp.dup_words, pb);
+          ok = poll_finish(a, vsrc, tbuf, shp.dup_words, (unsigned)step, pb, pt0);
         }
-        if (ok && w.n_probes > 0)
-          ok = poll_words(a, src, 0, w.n_probes, a.probes + w.probe_begin, nullptr, (unsigned)step, pt, npt);
         if (!ok) s_abort = 1;
       }
       __syncthreads();

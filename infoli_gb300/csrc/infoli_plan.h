@@ -95,6 +95,9 @@ typedef struct {
   int res_edges;   // resident edge offsets per CTA
   int edge_g;      // per-edge conductances present
   int stamped;     // stamped exchange (all tiles resident at once, nbuf = 1)
+  int dup_words;   // stamped: second copy of the window starts this many floats in
+                   // (a multiple of 32 plus 16, so each word sits in two banks 16
+                   // apart); 0 = single copy
 } SmemShape;
 
 // Number of per-cell float arrays kept in shared memory: V_dend, V_soma,

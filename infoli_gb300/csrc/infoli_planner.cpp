@@ -95,7 +95,8 @@ std::vector<TileSpan> make_tiles(const std::vector<int>& u, int cap, int n_pad) 
 // are rewritten to the lane-chunks (receiver-major, so a receiver's partial
 // sums stay contiguous and in sender order); the last group of a CTA is
 // filled with dummy chunks that write one spare slot.
-void pack_groups(Plan& P, const SmemLayout& L, const PlanInput& in, const std::vector<int>& starts) {
+void pack_groups(Plan& P, const SmemLayout& L, const PlanInput& in, const std::vector<int>& starts,
+                 int dup_words) {
   const bool edge_g = in.g != nullptr;
   std::vector<int2_t> gdesc;
   std::vector<uint16_t> pe;
@@ -179,13 +180,21 @@ void pack_groups(Plan& P, const SmemLayout& L, const PlanInput& in, const std::v
             const int wd = pad[l] >> 2;
             if (bank_word[wd & 31] < 0) bank_word[wd & 31] = wd;
           }
+        // an entry can be read from the first copy (bank b) or, when the
+        // window is duplicated, from the second (bank b + 16)
+        const unsigned dup_mask = dup_words ? 0xffffffffu : 0u;
+        auto banks_of = [&](uint16_t off) {
+          const int b2 = (off >> 2) & 31;
+          return (1u << b2) | (dup_mask & (1u << ((b2 + 16) & 31)));
+        };
+        unsigned taken = 0;  // banks already claimed by padding words
+        for (int b2 = 0; b2 < 32; ++b2)
+          if (bank_word[b2] >= 0) taken |= 1u << b2;
         unsigned adj[32];
         for (int l = 0; l < 32; ++l) {
           adj[l] = 0;
-          for (const auto& e : rem[l]) {
-            const int b2 = (e.first >> 2) & 31;
-            if (bank_word[b2] < 0) adj[l] |= 1u << b2;
-          }
+          for (const auto& e : rem[l]) adj[l] |= banks_of(e.first);
+          adj[l] &= ~taken;
         }
         int match_bank[32];  // bank -> lane
         for (int b2 = 0; b2 < 32; ++b2) match_bank[b2] = -1;
@@ -229,9 +238,14 @@ void pack_groups(Plan& P, const SmemLayout& L, const PlanInput& in, const std::v
         for (int l = 0; l < 32; ++l) {
           if (rem[l].empty()) continue;
           size_t q = 0;
-          if (lane_bank[l] >= 0)
-            while (((rem[l][q].first >> 2) & 31) != lane_bank[l]) ++q;
-          cell[l * kLaneEdges + k] = rem[l][q];
+          std::pair<uint16_t, float> pick = rem[l][0];
+          if (lane_bank[l] >= 0) {
+            while (!(banks_of(rem[l][q].first) & (1u << lane_bank[l]))) ++q;
+            pick = rem[l][q];
+            if (((pick.first >> 2) & 31) != lane_bank[l])  // the matched bank is the second copy's
+              pick.first = (uint16_t)(pick.first + sizeof(float) * (size_t)dup_words);
+          }
+          cell[l * kLaneEdges + k] = pick;
           rem[l].erase(rem[l].begin() + q);
         }
       }
@@ -483,16 +497,23 @@ bool make_plan(const PlanInput& in, Plan* out, std::string* err) {
     // stamped plans keep their work resident in the packed lane-chunk layout,
     // 16-bit byte offsets from the start of dynamic shared memory (so every
     // offset must stay below 64 KiB)
+    // Preferred: two copies of the window, the second 16 banks away, so every
+    // gather can pick the copy whose bank is free; else a single copy.
     SmemShape st = sh;
-    st.tile_cap = (sum_max + 3) & ~3;
-    st.nbuf = 1;
-    st.stamped = 1;
-    const SmemLayout SL0 = smem_layout(st);  // tile and cell-array offsets do not depend on the rest
-    const bool offsets_fit = SL0.vown + sizeof(float) * (size_t)cells_cap <= 65536;
-    Plan packed = P;
+    Plan packed;
     bool fits = false;
-    if (!in.no_resident && offsets_fit) {
-      pack_groups(packed, SL0, in, starts);
+    for (int dup = 1; dup >= 0 && !fits; --dup) {
+      st = sh;
+      st.nbuf = 1;
+      st.stamped = 1;
+      const int w4 = (sum_max + 3) & ~3;
+      st.dup_words = dup ? ((w4 + 31) & ~31) + 16 : 0;
+      st.tile_cap = dup ? st.dup_words + w4 : w4;
+      const SmemLayout SL0 = smem_layout(st);  // tile and cell-array offsets do not depend on the rest
+      const bool offsets_fit = SL0.vown + sizeof(float) * (size_t)cells_cap <= 65536;
+      if (in.no_resident || !offsets_fit) continue;
+      packed = P;
+      pack_groups(packed, SL0, in, starts, st.dup_words);
       int mg = 1;
       for (const CtaWork& w : packed.cta) mg = std::max(mg, w.n_groups);
       st.max_slots = packed.max_slots;
@@ -584,8 +605,14 @@ extern "C" int infoli_plan_emulate(int n, const int64_t* row_ptr, const int32_t*
       size_t toff = 0;
       for (int j = 0; j < w.n_tiles; ++j) {
         const TileDesc& td = P.tiles[w.tile_begin + j];
-        if (td.lo < 0 || td.lo % 4 || td.nfloats % 4 || toff + td.nfloats > (size_t)P.shape.tile_cap) return -4;
-        for (int i = 0; i < td.nfloats; ++i) fsm[toff + i] = (td.lo + i < n) ? vdend[td.lo + i] : 0.0f;
+        const size_t dup = (size_t)P.shape.dup_words;
+        if (td.lo < 0 || td.lo % 4 || td.nfloats % 4 || dup + toff + td.nfloats > (size_t)P.shape.tile_cap ||
+            (dup && toff + td.nfloats > dup))
+          return -4;
+        for (int i = 0; i < td.nfloats; ++i) {
+          fsm[toff + i] = (td.lo + i < n) ? vdend[td.lo + i] : 0.0f;
+          if (dup) fsm[dup + toff + i] = fsm[toff + i];
+        }
         toff += td.nfloats;
       }
       for (int q = 0; q < w.n_probes; ++q)
