@@ -131,6 +131,15 @@ int infoli_gen_fixed_degree(int n, int k, float g_lo, float g_hi, uint64_t seed,
 int infoli_bitmask_to_csr(int n, const uint32_t* bits, int64_t* row_ptr, int32_t* col, int64_t cap,
                           int64_t* n_edges);
 
+/* Dense random topology as a receiver bitmask (layout of
+ * infoli_bitmask_to_csr), the bitmask form of the reference's uniform
+ * generator (src/openmp/infoli.c:337-375) for the batched path: pair
+ * (r, s), s != r, is an edge when a 24-bit draw is below p * 2^24.  Receiver
+ * r draws from its own splitmix64 stream (state seed + (r + 1) * 0x632BE59BD9B4E019),
+ * one draw per sender in ascending order, so rows are generated in parallel
+ * and the result does not depend on the thread count. */
+int infoli_gen_bitmask(int n, float p, uint64_t seed, uint32_t* bits);
+
 /* ------------------------------------------------------------------------ */
 /* one simulation on the GPU                                                */
 /* ------------------------------------------------------------------------ */
@@ -212,6 +221,58 @@ int infoli_sim_set_profiling(infoli_sim* s, int on);
 int infoli_sim_get_profile(infoli_sim* s, double mean_ns[5], double max_ns[5]);
 
 int infoli_sim_destroy(infoli_sim* s);
+
+/* ------------------------------------------------------------------------ */
+/* many independent networks in one launch                                   */
+/* ------------------------------------------------------------------------ */
+
+/* No counterpart in the reference, which simulates one network per process
+ * (src/openmp/infoli.c:124-735); each network of a batch follows that
+ * process's step (same parameters, same explicit-Euler update, the uniform
+ * CONDUCTANCE of :320 as one conductance per network).  Networks are
+ * independent: no coupling between them. */
+typedef struct infoli_batch infoli_batch;
+
+typedef struct {
+  int n_nets;
+  const int* n_cells;        /* [n_nets] cells per network, each <= 8192 */
+  const float* params;       /* [INFOLI_NPARAM] shared by all networks */
+  /* [INFOLI_NSTATE * total] SoA over the networks' cells laid end to end
+   * (network 0's cells first), or NULL: broadcast init_values */
+  const float* init_state;
+  const float* init_values;  /* [INFOLI_NSTATE] */
+  /* receiver bitmasks laid end to end: network i (n = n_cells[i], w =
+   * ceil(n/32)) takes n * w words, row r = receiver r, bit s%32 of word s/32
+   * = sender s (infoli_gen_bitmask's layout); self bits and bits >= n are
+   * ignored */
+  const uint32_t* bits;
+  const float* g;            /* [n_nets] conductance of every edge of network i */
+  int flags;                 /* INFOLI_F_KAHAN */
+  int device;
+} infoli_batch_desc;
+
+/* Uploads the batch and packs it into thread-block clusters.  The stimulus
+ * defaults to the reference's pulse (6 uA/cm2, steps 20000 to 20498) on every
+ * cell of every network. */
+int infoli_batch_create(const infoli_batch_desc* desc, infoli_batch** out);
+int infoli_batch_set_stimulus_pulse(infoli_batch* b, int start_step, int end_step, float amp);
+/* Advances every network by n_steps steps in one kernel launch (replayed
+ * from a CUDA graph captured once per distinct n_steps); returns when done. */
+int infoli_batch_run(infoli_batch* b, int n_steps);
+/* out[INFOLI_NSTATE * total]: the state in init_state's layout. */
+int infoli_batch_get_state(infoli_batch* b, float* out);
+/* Replaces the state of every network (same layout); the step index and the
+ * stimulus schedule are kept. */
+int infoli_batch_set_state(infoli_batch* b, const float* in);
+/* Launch shape and the device time of the last run (any pointer may be NULL). */
+int infoli_batch_info(infoli_batch* b, int* ctas, int* cluster, int* block, int64_t* cells, float* last_ms);
+/* Per CTA of the launch (arrays of `ctas` entries, any may be NULL): the
+ * network it simulates (-1: idle slot of a cluster) and, for the last run,
+ * its start and end times in ns from the earliest CTA start;
+ * *max_active_clusters = clusters of this shape the device runs at once. */
+int infoli_batch_cta_info(infoli_batch* b, int* max_active_clusters, int32_t* net, int64_t* start_ns,
+                          int64_t* end_ns);
+int infoli_batch_destroy(infoli_batch* b);
 
 /* ------------------------------------------------------------------------ */
 /* allocation-free run                                                       */

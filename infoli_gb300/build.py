@@ -23,7 +23,7 @@ OUT = os.path.join(HERE, "_build")
 INC = os.path.join(os.path.dirname(HERE), "include")
 
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
-CU_SOURCES = ["infoli_kernels.cu", "infoli_capi.cu", "infoli_static.cu"]
+CU_SOURCES = ["infoli_kernels.cu", "infoli_capi.cu", "infoli_static.cu", "infoli_batch.cu"]
 CXX_SOURCES = ["infoli_planner.cpp"]
 C_SOURCES = ["infoli_host.c", "infoli_trace.c"]
 
@@ -62,7 +62,7 @@ def build(verbose: bool = False, force: bool = False) -> str:
         obj = os.path.join(OUT, f + ".o")
         objs.append(obj)
         if force or _stale(obj, [src] + headers):
-            jobs.append([nvcc, *ARCH, "-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC",
+            jobs.append([nvcc, *ARCH, "-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC,-fopenmp",
                          "-I", INC, "-c", src, "-o", obj])
     for f in CXX_SOURCES:
         src = os.path.join(SRC, f)

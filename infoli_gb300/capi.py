@@ -41,7 +41,10 @@ EXPORTED = [
     "infoli_sim_run_into", "infoli_sim_get_state", "infoli_sim_set_state", "infoli_sim_step",
     "infoli_sim_last_run_stats", "infoli_sim_plan_info", "infoli_sim_destroy", "infoli_format_f8",
     "infoli_format_row", "infoli_sim_set_profiling", "infoli_sim_get_profile", "infoli_plan_emulate",
-    "infoli_run_noalloc",
+    "infoli_run_noalloc", "infoli_gen_bitmask", "infoli_batch_create", "infoli_batch_set_stimulus_pulse",
+    "infoli_batch_run", "infoli_batch_get_state", "infoli_batch_set_state", "infoli_batch_info",
+    "infoli_batch_cta_info",
+    "infoli_batch_destroy",
 ]
 
 
@@ -61,6 +64,20 @@ class SimDesc(C.Structure):
         ("col", C.c_void_p),
         ("g", C.c_void_p),
         ("g_uniform", C.c_float),
+        ("flags", C.c_int),
+        ("device", C.c_int),
+    ]
+
+
+class BatchDesc(C.Structure):
+    _fields_ = [
+        ("n_nets", C.c_int),
+        ("n_cells", C.c_void_p),
+        ("params", C.c_void_p),
+        ("init_state", C.c_void_p),
+        ("init_values", C.c_void_p),
+        ("bits", C.c_void_p),
+        ("g", C.c_void_p),
         ("flags", C.c_int),
         ("device", C.c_int),
     ]
@@ -106,6 +123,15 @@ def load():
         "infoli_run_noalloc": ([P, I, P, P, P, F, I, I, F, P, I, I, P, P], I),
         "infoli_sim_set_profiling": ([P, I], I),
         "infoli_sim_get_profile": ([P, P, P], I),
+        "infoli_gen_bitmask": ([I, F, C.c_uint64, P], I),
+        "infoli_batch_create": ([C.POINTER(BatchDesc), C.POINTER(C.c_void_p)], I),
+        "infoli_batch_set_stimulus_pulse": ([P, I, I, F], I),
+        "infoli_batch_run": ([P, I], I),
+        "infoli_batch_get_state": ([P, P], I),
+        "infoli_batch_set_state": ([P, P], I),
+        "infoli_batch_info": ([P, P, P, P, P, P], I),
+        "infoli_batch_cta_info": ([P, P, P, P, P], I),
+        "infoli_batch_destroy": ([P], I),
         "infoli_format_f8": ([C.c_char_p, F], I),
         "infoli_format_row": ([C.c_char_p, I64, P, I, I, I], I64),
     }
@@ -345,3 +371,98 @@ class Simulation:
                                             C.byref(sm)))
         return {"grid": g.value, "threads": t.value, "tiles": ti.value, "chunks": ch.value,
                 "smem_bytes": sm.value}
+
+
+def gen_bitmask(n: int, p: float, seed: int) -> np.ndarray:
+    """Receiver bitmask [n, ceil(n/32)] uint32 (include/infoli_gpu.h: infoli_gen_bitmask)."""
+    bits = np.zeros((n, (n + 31) // 32), dtype=np.uint32)
+    _check(load().infoli_gen_bitmask(int(n), float(p), int(seed) & (2**64 - 1), _p(bits)))
+    return bits
+
+
+class Batch:
+    """Many independent networks in one launch (infoli_batch_* handle).
+
+    nets: list of (n_cells, bits[n, ceil(n/32)] uint32, g) per network.
+    init_state: [NSTATE, total] over the networks' cells end to end, or None
+    (then init_values is broadcast)."""
+
+    def __init__(self, params, nets, init_state=None, init_values=None, kahan=False, device=0):
+        L = load()
+        self._L = L
+        params = np.ascontiguousarray(params, dtype=np.float32)
+        assert params.size >= NPARAM
+        self.params = params[:NPARAM].copy()
+        self.sizes = np.array([int(n) for n, _, _ in nets], dtype=np.int32)
+        self.offsets = np.concatenate([[0], np.cumsum(self.sizes, dtype=np.int64)])
+        self.total = int(self.offsets[-1])
+        self._bits = np.concatenate([np.ascontiguousarray(b, dtype=np.uint32).ravel() for _, b, _ in nets])
+        self._g = np.array([float(g) for _, _, g in nets], dtype=np.float32)
+        d = BatchDesc()
+        d.n_nets = len(nets)
+        d.n_cells = _p(self.sizes)
+        d.params = _p(self.params)
+        if init_state is not None:
+            self._st = np.ascontiguousarray(init_state, dtype=np.float32).reshape(NSTATE, self.total)
+            d.init_state = _p(self._st)
+        else:
+            self._iv = np.ascontiguousarray(init_values, dtype=np.float32)
+            assert self._iv.size == NSTATE
+            d.init_values = _p(self._iv)
+        d.bits = _p(self._bits)
+        d.g = _p(self._g)
+        d.flags = F_KAHAN if kahan else 0
+        d.device = int(device)
+        h = C.c_void_p()
+        _check(L.infoli_batch_create(C.byref(d), C.byref(h)))
+        self._h = h
+
+    def close(self):
+        if getattr(self, "_h", None):
+            self._L.infoli_batch_destroy(self._h)
+            self._h = None
+
+    __del__ = close
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *exc):
+        self.close()
+
+    def set_stimulus_pulse(self, start, end, amp):
+        _check(self._L.infoli_batch_set_stimulus_pulse(self._h, int(start), int(end), float(amp)))
+
+    def run(self, n_steps):
+        _check(self._L.infoli_batch_run(self._h, int(n_steps)))
+
+    def get_state(self) -> np.ndarray:
+        out = np.zeros((NSTATE, self.total), dtype=np.float32)
+        _check(self._L.infoli_batch_get_state(self._h, _p(out)))
+        return out
+
+    def set_state(self, st):
+        st = np.ascontiguousarray(st, dtype=np.float32).reshape(NSTATE, self.total)
+        _check(self._L.infoli_batch_set_state(self._h, _p(st)))
+
+    def net_state(self, st: np.ndarray, i: int) -> np.ndarray:
+        return st[:, self.offsets[i]:self.offsets[i + 1]]
+
+    def info(self):
+        ctas, cl, blk = C.c_int(), C.c_int(), C.c_int()
+        cells = C.c_int64()
+        ms = C.c_float()
+        _check(self._L.infoli_batch_info(self._h, C.byref(ctas), C.byref(cl), C.byref(blk), C.byref(cells),
+                                         C.byref(ms)))
+        return {"ctas": ctas.value, "cluster": cl.value, "block": blk.value, "cells": cells.value,
+                "last_ms": ms.value}
+
+    def cta_info(self):
+        """{"max_active_clusters", "net"[ctas], "start_ns"[ctas], "end_ns"[ctas]} of the last run."""
+        k = self.info()["ctas"]
+        mac = C.c_int()
+        net = np.zeros(k, np.int32)
+        t0 = np.zeros(k, np.int64)
+        t1 = np.zeros(k, np.int64)
+        _check(self._L.infoli_batch_cta_info(self._h, C.byref(mac), _p(net), _p(t0), _p(t1)))
+        return {"max_active_clusters": mac.value, "net": net, "start_ns": t0, "end_ns": t1}

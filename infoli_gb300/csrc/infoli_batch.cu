@@ -1,0 +1,726 @@
+// Batched simulation of many independent networks in one captured graph.
+//
+// Each network's cells are split over the CTAs of ONE thread-block cluster
+// (up to 8 CTAs of 1024 threads; one thread per cell, state in registers).
+// Every CTA keeps the whole network's V_dend, double-buffered, in its shared
+// memory; a new V_dend is written to the CTA's own copy and, through
+// distributed shared memory, to the copies of the network's other CTAs, and
+// the cluster's hardware barrier separates the steps.  No grid-wide
+// synchronisation: every cluster runs its network independently.  Networks
+// needing the same number of CTAs form one launch with that cluster size, so
+// clusters have no idle CTA; the launches run concurrently.
+//
+// Coupling is read from per-network adjacency bitmasks with one conductance
+// per network (the reference's uniform CONDUCTANCE, src/openmp/infoli.c:320):
+// a receiver walks the set bits of its row (src/openmp/infoli.c:512-518 for
+// the arithmetic).  Rows are stored word-major so consecutive receivers read
+// consecutive words; a network whose rows fit keeps them in shared memory for
+// the launch, otherwise they are streamed from global memory every step.
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <cstdint>
+#include <cstdlib>
+#include <cstring>
+#include <vector>
+
+#include "../../include/infoli_gpu.h"
+#include "infoli_cell.cuh"
+#include "infoli_internal.h"
+#include "infoli_ptx.cuh"
+
+namespace infoli {
+namespace {
+
+constexpr float kNegLog2eOver100 = -0.014426950408889634f;  // -log2(e)/100
+
+// One CTA slot of a cluster.
+struct alignas(16) BatchCta {
+  int net;           // network, -1: idle slot
+  int rank;          // rank of this CTA inside its network (0 .. ncta-1)
+  int ncta;          // CTAs of the network
+  int rank0;         // cluster rank of the network's first CTA (ranks are contiguous)
+  int cbeg, ncell;   // owned cells [cbeg, cbeg + ncell), network-local
+  int n;             // cells in the network
+  int wpr;           // bitmask words per receiver row, ceil(n / 32)
+  long long cell_base;  // first cell of the network in the concatenated state arrays
+  long long bits_base;  // word w of receiver r at bits[bits_base + w * n + r]
+  float g;           // conductance of every edge of the network
+  int resident;      // rows of the owned receivers kept in shared memory
+  int cl_sync;       // the cluster holds a network of several CTAs: cluster barrier per step
+  int pad0;
+};
+
+struct BatchArgs {
+  ModelParams P;
+  const BatchCta* cta;
+  const uint32_t* bits;
+  float* st;         // INFOLI_NSTATE x total SoA (reference order); Ca2+ row unused
+  double* ca;        // Ca2+ concentration per cell, kept in FP64 between launches
+  long long total;   // cells in the batch
+  int vcap;          // floats per V buffer in shared memory
+  int res_words;     // shared words for resident rows (per CTA)
+  const int* step;   // current step index of the batch (device)
+  int n_steps;
+  int pulse_start, pulse_end;
+  float pulse_amp;
+  unsigned long long* cta_ns;  // [2 * grid]: globaltimer at start and end of every CTA
+};
+
+__device__ __forceinline__ void cluster_sync_all() {
+  asm volatile("barrier.cluster.arrive.release.aligned;\n\tbarrier.cluster.wait.acquire.aligned;" ::: "memory");
+}
+
+__device__ __forceinline__ unsigned cluster_rank() {
+  unsigned r;
+  asm volatile("mov.u32 %0, %%cluster_ctarank;" : "=r"(r));
+  return r;
+}
+
+// Store a float into the shared memory of CTA `peer` of this cluster at the
+// address that `local` has in this CTA.
+__device__ __forceinline__ void st_peer(float* local, unsigned peer, float v) {
+  const unsigned la = smem_u32(local);
+  unsigned ra;
+  asm volatile("mapa.shared::cluster.u32 %0, %1, %2;" : "=r"(ra) : "r"(la), "r"(peer));
+  asm volatile("st.shared::cluster.f32 [%0], %1;" ::"r"(ra), "f"(v) : "memory");
+}
+
+// Predicated word loads: when `take` is false the destination keeps its value
+// and nothing is read (no branch, so lanes that refill and lanes that do not
+// stay converged).
+__device__ __forceinline__ void ld_shared_if(uint32_t& dst, uint32_t saddr, bool take) {
+  asm volatile("{\n\t.reg .pred p;\n\tsetp.ne.u32 p, %2, 0;\n\t@p ld.shared.u32 %0, [%1];\n\t}"
+               : "+r"(dst)
+               : "r"(saddr), "r"((unsigned)take));
+}
+__device__ __forceinline__ void ld_global_if(uint32_t& dst, const uint32_t* gaddr, bool take) {
+  asm volatile("{\n\t.reg .pred p;\n\tsetp.ne.u32 p, %2, 0;\n\t@p ld.global.nc.u32 %0, [%1];\n\t}"
+               : "+r"(dst)
+               : "l"(gaddr), "r"((unsigned)take));
+}
+__device__ __forceinline__ float ld_shared_f32(uint32_t saddr) {
+  float v;
+  asm volatile("ld.shared.f32 %0, [%1];" : "=f"(v) : "r"(saddr));
+  return v;
+}
+
+template <bool KAHAN>
+__device__ __forceinline__ void add_edge(float& acc, float& cmp, float vc, float vs, bool live) {
+  const float V = vc - vs;
+  const float f = fmaf(0.8f, ex2_approx((V * V) * kNegLog2eOver100), 0.2f);
+  const float term = live ? f * V : 0.0f;
+  if (KAHAN) {
+    const float y = term - cmp;
+    const float s = acc + y;
+    cmp = (s - acc) - y;
+    acc = s;
+  } else {
+    acc += term;
+  }
+}
+
+// Gap-junction currents of a warp's 32 receivers from their bitmask rows,
+// one 32-sender column of the rows at a time.  Words are stored
+// most-significant-bit first (bit 31 of word w = sender 32 w), so a count of
+// leading zeros is the sender's offset within the column.  For each column
+// the warp runs as many iterations as the fullest word of its lanes has bits
+// (a warp-wide max of the popcounts); an iteration takes the next set bit of
+// every lane's word and reads that sender's V_dend.  All lanes read from the
+// same 32 consecutive floats, so the reads never conflict on a shared-memory
+// bank, and the loop has no divergent branch.  A lane whose word is used up
+// reads a float past the column (inside the V_dend buffer's 32-float tail
+// pad) and adds nothing.  Senders are visited in ascending order (the
+// reference's order); the terms of a column are summed in FP32 and, with
+// KAHAN, the column sums are added with Kahan compensation.  Lanes without a
+// receiver pass own == false.
+//   RES: words in shared memory at byte address wsm + 4 * BLOCK * w;
+//   else words in global memory at gw[w * stride].
+template <bool KAHAN, bool RES>
+__device__ __forceinline__ float couple_warp(bool own, uint32_t wsm, uint32_t wstride_b, const uint32_t* gw,
+                                            uint32_t stride, int wpr, uint32_t vbase, float vc) {
+  float acc = 0.0f, cmp = 0.0f;
+  uint32_t nx = 0u, nnx = 0u;
+  if (own) {
+    if (RES) {
+      ld_shared_if(nx, wsm, true);
+      ld_shared_if(nnx, wsm + wstride_b, wpr > 1);
+    } else {
+      nx = __ldg(gw);
+      if (wpr > 1) nnx = __ldg(gw + stride);
+    }
+  }
+  for (int w = 0; w < wpr; ++w) {
+    uint32_t x = nx;
+    nx = nnx;
+    // words w + 2 are loaded two columns ahead (rows end with two zero words)
+    if (RES)
+      ld_shared_if(nnx, wsm + (uint32_t)(w + 2) * wstride_b, own);
+    else
+      ld_global_if(nnx, gw + (size_t)(w + 2) * stride, own);
+    const int m = (int)__reduce_max_sync(0xffffffffu, (unsigned)__popc(x));
+    const uint32_t vcol = vbase + 128u * (uint32_t)w;
+    float col = 0.0f;  // this column's terms (at most 32)
+    for (int k = 0; k < m; ++k) {
+      const int c = __clz(x);  // 32 once x is used up
+      const bool live = x != 0u;
+      x &= __funnelshift_rc(0x7fffffffu, 0u, (unsigned)c);
+      const float V = vc - ld_shared_f32(vcol + 4u * (uint32_t)c);
+      const float f = fmaf(0.8f, ex2_approx((V * V) * kNegLog2eOver100), 0.2f);
+      if (live) col = fmaf(f, V, col);
+    }
+    if (KAHAN) {
+      // compensated sum over the column sums
+      const float y = col - cmp;
+      const float s = acc + y;
+      cmp = (s - acc) - y;
+      acc = s;
+    } else {
+      acc += col;
+    }
+  }
+  return acc;
+}
+
+template <int BLOCK, bool KAHAN>
+__global__ void __launch_bounds__(BLOCK, 1) batch_kernel(const __grid_constant__ BatchArgs a) {
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  float* vbuf = reinterpret_cast<float*>(smem_raw);              // [2][vcap]
+  uint32_t* sbits = reinterpret_cast<uint32_t*>(vbuf + 2 * a.vcap);  // [wpr + 2][BLOCK] if resident
+  const unsigned long long t_start = globaltimer_ns();
+  const BatchCta w = a.cta[blockIdx.x];
+  const int tid = threadIdx.x;
+  const unsigned me = cluster_rank();
+  const bool own = w.net >= 0 && tid < w.ncell;
+  const int r = w.cbeg + tid;
+  const long long gc = w.cell_base + r;
+  const long long T = a.total;
+  const int step0 = *a.step;
+
+  Volts v{};
+  Gates gs{};
+  if (own) {
+    const float* s = a.st;
+    v.Vd = s[0 * T + gc];
+    gs.r = s[1 * T + gc];
+    gs.s = s[2 * T + gc];
+    gs.q = s[3 * T + gc];
+    gs.Ca = a.ca[gc];
+    gs.ICaH = s[5 * T + gc];
+    gs.gCaL = s[6 * T + gc];
+    v.Vs = s[7 * T + gc];
+    gs.m = s[8 * T + gc];
+    gs.h = s[9 * T + gc];
+    gs.n = s[10 * T + gc];
+    gs.p = s[11 * T + gc];
+    gs.xs = s[12 * T + gc];
+    gs.k = s[13 * T + gc];
+    gs.l = s[14 * T + gc];
+    v.Va = s[15 * T + gc];
+    gs.ma = s[16 * T + gc];
+    gs.ha = s[17 * T + gc];
+    gs.xa = s[18 * T + gc];
+  }
+  if (w.net >= 0 && w.resident) {
+    for (int i = tid; i < (w.wpr + 2) * BLOCK; i += BLOCK) {
+      const int ww = i / BLOCK, rr = i % BLOCK;
+      sbits[i] = rr < w.ncell ? a.bits[w.bits_base + (long long)ww * w.n + w.cbeg + rr] : 0u;
+    }
+  }
+  cluster_sync_all();  // every CTA of the cluster is running before peers write into it
+  if (own) {
+    vbuf[r] = v.Vd;
+    for (int p = 0; p < w.ncta; ++p)
+      if (w.rank0 + p != (int)me) st_peer(vbuf + r, (unsigned)(w.rank0 + p), v.Vd);
+  }
+  cluster_sync_all();
+
+  const VoltCoef vk = volt_coef(a.P);
+  for (int t = 0; t < a.n_steps; ++t) {
+    const int step = step0 + t;
+    const float* vcur = vbuf + (t & 1) * a.vcap;
+    float* vnxt = vbuf + ((t + 1) & 1) * a.vcap;
+    // ---- coupling: the set bits of the rows (whole warps, owned or not)
+    float sum = 0.0f;
+    if (w.net >= 0 && (tid & ~31) < w.ncell) {
+      const uint32_t vbase = smem_u32(vcur);
+      sum = w.resident ? couple_warp<KAHAN, true>(own, smem_u32(sbits + tid), 4u * BLOCK, nullptr, 0u, w.wpr, vbase,
+                                                  v.Vd)
+                       : couple_warp<KAHAN, false>(own, 0u, 0u, a.bits + w.bits_base + r, (uint32_t)w.n, w.wpr,
+                                                   vbase, v.Vd);
+    }
+    if (own) {
+      const float ic = sum * w.g;
+      const float iapp = (step >= a.pulse_start && step < a.pulse_end) ? a.pulse_amp : 0.0f;
+      // ---- fused compartment update
+      Currents cur;
+      run_units(a.P, 0xffu, v, gs, cur);
+      voltage_step(a.P, vk, v, cur, ic, iapp);
+      vnxt[r] = v.Vd;
+      for (int p = 0; p < w.ncta; ++p)
+        if (w.rank0 + p != (int)me) st_peer(vnxt + r, (unsigned)(w.rank0 + p), v.Vd);
+    }
+    if (w.cl_sync)
+      cluster_sync_all();
+    else
+      __syncthreads();
+  }
+
+  if (own) {
+    float* s = a.st;
+    s[0 * T + gc] = v.Vd;
+    s[1 * T + gc] = gs.r;
+    s[2 * T + gc] = gs.s;
+    s[3 * T + gc] = gs.q;
+    a.ca[gc] = gs.Ca;
+    s[5 * T + gc] = gs.ICaH;
+    s[7 * T + gc] = v.Vs;
+    s[8 * T + gc] = gs.m;
+    s[9 * T + gc] = gs.h;
+    s[10 * T + gc] = gs.n;
+    s[11 * T + gc] = gs.p;
+    s[12 * T + gc] = gs.xs;
+    s[13 * T + gc] = gs.k;
+    s[14 * T + gc] = gs.l;
+    s[15 * T + gc] = v.Va;
+    s[16 * T + gc] = gs.ma;
+    s[17 * T + gc] = gs.ha;
+    s[18 * T + gc] = gs.xa;
+  }
+  if (tid == 0) {
+    a.cta_ns[2 * blockIdx.x] = t_start;
+    a.cta_ns[2 * blockIdx.x + 1] = globaltimer_ns();
+  }
+}
+
+__global__ void batch_advance(int* step, int n) {
+  if (threadIdx.x == 0 && blockIdx.x == 0) *step += n;
+}
+
+}  // namespace
+}  // namespace infoli
+
+using namespace infoli;
+
+namespace {
+
+// Networks that need the same number of CTAs form a group; a group is one
+// kernel launch whose clusters have exactly that many CTAs, one network per
+// cluster, so no cluster has an idle CTA.  The groups run concurrently (one
+// stream each, forked and joined inside the captured graph), the groups of
+// the largest networks first and at the highest priority.
+struct BatchGroup {
+  int cs = 1;             // CTAs per cluster = CTAs per network
+  int cta_off = 0, grid = 0;
+  int vcap = 0, res_words = 0;
+  size_t smem = 0;
+  int max_active = 0;     // clusters of this group the device runs at once
+  int priority = 0;
+  cudaStream_t stream = nullptr;
+  cudaEvent_t done = nullptr;
+};
+
+}  // namespace
+
+struct infoli_batch {
+  int device = 0;
+  int n_nets = 0;
+  long long total = 0;
+  ModelParams P{};
+  int kahan = 0;
+  int block = 1024;
+  std::vector<BatchGroup> groups;
+  std::vector<BatchCta> cta;
+  std::vector<long long> cell_base;
+  BatchCta* d_cta = nullptr;
+  uint32_t* d_bits = nullptr;
+  float* d_st = nullptr;
+  double* d_ca = nullptr;
+  int* d_step = nullptr;
+  unsigned long long* d_cta_ns = nullptr;
+  int pulse_start = 20000, pulse_end = 20499;
+  float pulse_amp = 6.0f;
+  cudaStream_t stream = nullptr;
+  cudaEvent_t fork = nullptr;
+  cudaGraph_t graph = nullptr;
+  cudaGraphExec_t graph_exec = nullptr;
+  int graph_steps = -1;
+  cudaEvent_t ev0 = nullptr, ev1 = nullptr;
+  float last_ms = 0;
+};
+
+namespace {
+
+#define BK(call)                                                                                   \
+  do {                                                                                             \
+    cudaError_t e_ = (call);                                                                       \
+    if (e_ != cudaSuccess)                                                                         \
+      return infoli__fail(INFOLI_ERR_CUDA, "%s: %s (%s:%d)", #call, cudaGetErrorString(e_), __FILE__, \
+                          __LINE__);                                                               \
+  } while (0)
+
+uint32_t reverse_bits(uint32_t x) {
+  x = ((x >> 1) & 0x55555555u) | ((x & 0x55555555u) << 1);
+  x = ((x >> 2) & 0x33333333u) | ((x & 0x33333333u) << 2);
+  x = ((x >> 4) & 0x0F0F0F0Fu) | ((x & 0x0F0F0F0Fu) << 4);
+  x = ((x >> 8) & 0x00FF00FFu) | ((x & 0x00FF00FFu) << 8);
+  return (x >> 16) | (x << 16);
+}
+
+void batch_release(infoli_batch* b) {
+  if (!b) return;
+  cudaSetDevice(b->device);
+  if (b->stream) cudaStreamSynchronize(b->stream);
+  if (b->graph_exec) cudaGraphExecDestroy(b->graph_exec);
+  if (b->graph) cudaGraphDestroy(b->graph);
+  for (void* p : {(void*)b->d_cta, (void*)b->d_bits, (void*)b->d_st, (void*)b->d_ca, (void*)b->d_step,
+                  (void*)b->d_cta_ns})
+    if (p) cudaFree(p);
+  for (BatchGroup& g : b->groups) {
+    if (g.done) cudaEventDestroy(g.done);
+    if (g.stream) cudaStreamDestroy(g.stream);
+  }
+  if (b->fork) cudaEventDestroy(b->fork);
+  if (b->ev0) cudaEventDestroy(b->ev0);
+  if (b->ev1) cudaEventDestroy(b->ev1);
+  if (b->stream) cudaStreamDestroy(b->stream);
+  delete b;
+}
+
+const void* kernel_ptr(int block, bool kahan) {
+  if (block == 512) return kahan ? (const void*)batch_kernel<512, true> : (const void*)batch_kernel<512, false>;
+  return kahan ? (const void*)batch_kernel<1024, true> : (const void*)batch_kernel<1024, false>;
+}
+
+// Kernel attributes are set before any capture (cudaFuncSetAttribute is not a
+// stream operation).
+cudaError_t set_attrs(int block, size_t smem, int cluster) {
+  for (int k = 0; k < 2; ++k) {
+    const void* fn = kernel_ptr(block, k == 1);
+    cudaError_t e = cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    if (e == cudaSuccess && cluster > 8) e = cudaFuncSetAttribute(fn, cudaFuncAttributeNonPortableClusterSizeAllowed, 1);
+    if (e != cudaSuccess) return e;
+  }
+  return cudaSuccess;
+}
+
+void fill_config(cudaLaunchConfig_t& cfg, cudaLaunchAttribute* at, int grid, int block, int cluster, size_t smem,
+                 int priority, cudaStream_t s) {
+  cfg = cudaLaunchConfig_t{};
+  cfg.gridDim = dim3(grid);
+  cfg.blockDim = dim3(block);
+  cfg.dynamicSmemBytes = smem;
+  cfg.stream = s;
+  at[0].id = cudaLaunchAttributeClusterDimension;
+  at[0].val.clusterDim.x = cluster;
+  at[0].val.clusterDim.y = 1;
+  at[0].val.clusterDim.z = 1;
+  at[1].id = cudaLaunchAttributePriority;
+  at[1].val.priority = priority;
+  cfg.attrs = at;
+  cfg.numAttrs = 2;
+}
+
+int max_clusters(int block, int cluster, size_t smem) {
+  cudaLaunchConfig_t cfg;
+  cudaLaunchAttribute at[2];
+  fill_config(cfg, at, cluster, block, cluster, smem, 0, nullptr);
+  cfg.numAttrs = 1;
+  int n = 0;
+  if (cudaOccupancyMaxActiveClusters(&n, kernel_ptr(block, false), &cfg) != cudaSuccess) return 0;
+  return n;
+}
+
+cudaError_t launch_group(const infoli_batch* b, const BatchGroup& g, BatchArgs a) {
+  a.cta += g.cta_off;
+  a.cta_ns += 2 * (size_t)g.cta_off;
+  a.vcap = g.vcap;
+  a.res_words = g.res_words;
+  cudaLaunchConfig_t cfg;
+  cudaLaunchAttribute at[2];
+  fill_config(cfg, at, g.grid, b->block, g.cs, g.smem, g.priority, g.stream);
+  if (b->block == 512)
+    return b->kahan ? cudaLaunchKernelEx(&cfg, batch_kernel<512, true>, a)
+                    : cudaLaunchKernelEx(&cfg, batch_kernel<512, false>, a);
+  return b->kahan ? cudaLaunchKernelEx(&cfg, batch_kernel<1024, true>, a)
+                  : cudaLaunchKernelEx(&cfg, batch_kernel<1024, false>, a);
+}
+
+}  // namespace
+
+extern "C" int infoli_batch_create(const infoli_batch_desc* d, infoli_batch** out) {
+  infoli__clear_error();
+  if (!d || !out || d->n_nets <= 0 || !d->n_cells || !d->params || !d->bits || !d->g ||
+      (!d->init_state && !d->init_values))
+    return infoli__fail(INFOLI_ERR_ARG, "batch_create: bad argument");
+  *out = nullptr;
+  infoli_batch* b = new infoli_batch();
+  auto fail = [&](int rc) {
+    batch_release(b);
+    return rc;
+  };
+  b->device = d->device;
+  b->n_nets = d->n_nets;
+  b->kahan = (d->flags & INFOLI_F_KAHAN) ? 1 : 0;
+  std::memcpy(&b->P, d->params, sizeof(ModelParams));
+  if (cudaSetDevice(b->device) != cudaSuccess) return fail(infoli__fail(INFOLI_ERR_CUDA, "cudaSetDevice failed"));
+  const char* shape_env = getenv("INFOLI_BATCH_SHAPE");
+  b->block = (shape_env && atoi(shape_env) == 512) ? 512 : 1024;
+  const int max_cs = b->block == 1024 ? 8 : 16;
+  b->cell_base.resize(d->n_nets);
+  long long bits_total = 0, in_total = 0;
+  std::vector<long long> bits_base(d->n_nets), in_base(d->n_nets);
+  for (int i = 0; i < d->n_nets; ++i) {
+    const int n = d->n_cells[i];
+    if (n <= 0) return fail(infoli__fail(INFOLI_ERR_ARG, "batch_create: network %d has no cells", i));
+    if ((n + b->block - 1) / b->block > max_cs)
+      return fail(infoli__fail(INFOLI_ERR_CAPACITY, "batch_create: network %d has %d cells (at most %d)", i, n,
+                               b->block * max_cs));
+    b->cell_base[i] = b->total;
+    b->total += n;
+    in_base[i] = in_total;
+    in_total += (long long)n * ((n + 31) / 32);
+    bits_base[i] = bits_total;
+    bits_total += (long long)n * ((n + 31) / 32 + 2);
+  }
+  // time per step of a network ~ its mean row weight (set bits per receiver)
+  // plus a constant for the cell update: heavy networks are launched first
+  std::vector<double> weight(d->n_nets);
+#pragma omp parallel for schedule(dynamic, 1)
+  for (int i = 0; i < d->n_nets; ++i) {
+    const int n = d->n_cells[i], wpr = (n + 31) / 32;
+    const uint32_t* src = d->bits + in_base[i];
+    long long ones = 0;
+    for (long long k = 0; k < (long long)n * wpr; ++k) ones += __builtin_popcount(src[k]);
+    weight[i] = (double)ones / n + 64.0;
+  }
+  int smem_optin = 0, prio_lo = 0, prio_hi = 0;
+  cudaDeviceGetAttribute(&smem_optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, b->device);
+  cudaDeviceGetStreamPriorityRange(&prio_lo, &prio_hi);
+  const size_t budget = (size_t)smem_optin - 1024;
+  for (int cs = max_cs; cs >= 1; --cs) {
+    std::vector<int> nets;
+    for (int i = 0; i < d->n_nets; ++i)
+      if ((d->n_cells[i] + b->block - 1) / b->block == cs) nets.push_back(i);
+    if (nets.empty()) continue;
+    std::stable_sort(nets.begin(), nets.end(), [&](int x, int y) { return weight[x] > weight[y]; });
+    BatchGroup g;
+    g.cs = cs;
+    g.cta_off = (int)b->cta.size();
+    int nmax = 0;
+    for (int i : nets) nmax = std::max(nmax, d->n_cells[i]);
+    g.vcap = ((nmax + 31) / 32) * 32 + 32;  // + the 32-float pad read by finished lanes
+    const size_t vbytes = 2 * sizeof(float) * (size_t)g.vcap;
+    int res_rows = 0;  // words per resident row (wpr + 2), max over resident networks
+    for (int i : nets) {
+      const int wr = (d->n_cells[i] + 31) / 32 + 2;
+      if (vbytes + sizeof(uint32_t) * (size_t)wr * b->block <= budget) res_rows = std::max(res_rows, wr);
+    }
+    g.res_words = res_rows * b->block;
+    g.smem = vbytes + sizeof(uint32_t) * (size_t)g.res_words;
+    if (g.smem > budget)
+      return fail(infoli__fail(INFOLI_ERR_CAPACITY, "batch_create: %zu bytes of shared memory needed", g.smem));
+    if (set_attrs(b->block, budget, max_cs) != cudaSuccess || (g.max_active = max_clusters(b->block, cs, g.smem)) <= 0)
+      return fail(infoli__fail(INFOLI_ERR_CAPACITY, "batch_create: clusters of %d CTAs of %d threads cannot run",
+                               cs, b->block));
+    // greatest priority for the largest networks
+    g.priority = std::max(prio_hi, std::min(prio_lo, prio_hi + (max_cs - cs) * (prio_lo - prio_hi) / max_cs));
+    for (int i : nets) {
+      const int n = d->n_cells[i];
+      const int per = (n + cs - 1) / cs;
+      for (int k = 0; k < cs; ++k) {
+        BatchCta w{};
+        w.net = i;
+        w.rank = k;
+        w.ncta = cs;
+        w.rank0 = 0;
+        w.cbeg = std::min(n, k * per);
+        w.ncell = std::min(n, (k + 1) * per) - w.cbeg;
+        w.n = n;
+        w.wpr = (n + 31) / 32;
+        w.cell_base = b->cell_base[i];
+        w.bits_base = bits_base[i];
+        w.g = d->g[i];
+        w.resident = (w.wpr + 2) * b->block <= g.res_words ? 1 : 0;
+        w.cl_sync = cs > 1 ? 1 : 0;
+        b->cta.push_back(w);
+      }
+    }
+    g.grid = (int)b->cta.size() - g.cta_off;
+    b->groups.push_back(g);
+  }
+
+  // Device bitmasks, word-major (word w of receiver r at base + w * n + r),
+  // most-significant bit first, two zero words after every row.
+  std::vector<uint32_t> tb((size_t)bits_total, 0u);
+#pragma omp parallel for schedule(dynamic, 1)
+  for (int i = 0; i < d->n_nets; ++i) {
+    const int n = d->n_cells[i], wpr = (n + 31) / 32;
+    const uint32_t* src = d->bits + in_base[i];
+    uint32_t* dst = tb.data() + bits_base[i];
+    for (int r = 0; r < n; ++r)
+      for (int wd = 0; wd < wpr; ++wd) {
+        uint32_t x = src[(size_t)r * wpr + wd];
+        if (wd == r / 32) x &= ~(1u << (r % 32));  // no self-coupling
+        if (wd == wpr - 1 && n % 32) x &= (1u << (n % 32)) - 1u;
+        dst[(size_t)wd * n + r] = reverse_bits(x);
+      }
+  }
+  std::vector<float> st((size_t)INFOLI_NSTATE * b->total);
+  if (d->init_state) {
+    std::memcpy(st.data(), d->init_state, st.size() * sizeof(float));
+  } else {
+    for (int k = 0; k < INFOLI_NSTATE; ++k)
+      std::fill(st.begin() + (size_t)k * b->total, st.begin() + (size_t)(k + 1) * b->total, d->init_values[k]);
+  }
+  std::vector<double> ca(st.begin() + 4 * b->total, st.begin() + 5 * b->total);
+  if (cudaMalloc((void**)&b->d_cta, sizeof(BatchCta) * b->cta.size()) != cudaSuccess ||
+      cudaMalloc((void**)&b->d_bits, sizeof(uint32_t) * std::max<size_t>(1, tb.size())) != cudaSuccess ||
+      cudaMalloc((void**)&b->d_st, sizeof(float) * st.size()) != cudaSuccess ||
+      cudaMalloc((void**)&b->d_ca, sizeof(double) * b->total) != cudaSuccess ||
+      cudaMalloc((void**)&b->d_step, sizeof(int)) != cudaSuccess ||
+      cudaMalloc((void**)&b->d_cta_ns, sizeof(unsigned long long) * 2 * b->cta.size()) != cudaSuccess)
+    return fail(infoli__fail(INFOLI_ERR_NOMEM, "batch_create: device allocation failed"));
+  if (cudaMemcpy(b->d_cta, b->cta.data(), sizeof(BatchCta) * b->cta.size(), cudaMemcpyHostToDevice) != cudaSuccess ||
+      cudaMemcpy(b->d_bits, tb.data(), sizeof(uint32_t) * tb.size(), cudaMemcpyHostToDevice) != cudaSuccess ||
+      cudaMemcpy(b->d_st, st.data(), sizeof(float) * st.size(), cudaMemcpyHostToDevice) != cudaSuccess ||
+      cudaMemcpy(b->d_ca, ca.data(), sizeof(double) * ca.size(), cudaMemcpyHostToDevice) != cudaSuccess ||
+      cudaMemset(b->d_step, 0, sizeof(int)) != cudaSuccess ||
+      cudaMemset(b->d_cta_ns, 0, sizeof(unsigned long long) * 2 * b->cta.size()) != cudaSuccess)
+    return fail(infoli__fail(INFOLI_ERR_CUDA, "batch_create: upload failed"));
+  if (cudaStreamCreateWithFlags(&b->stream, cudaStreamNonBlocking) != cudaSuccess ||
+      cudaEventCreateWithFlags(&b->fork, cudaEventDisableTiming) != cudaSuccess ||
+      cudaEventCreate(&b->ev0) != cudaSuccess || cudaEventCreate(&b->ev1) != cudaSuccess)
+    return fail(infoli__fail(INFOLI_ERR_CUDA, "batch_create: stream/event creation failed"));
+  for (BatchGroup& g : b->groups)
+    if (cudaStreamCreateWithPriority(&g.stream, cudaStreamNonBlocking, g.priority) != cudaSuccess ||
+        cudaEventCreateWithFlags(&g.done, cudaEventDisableTiming) != cudaSuccess)
+      return fail(infoli__fail(INFOLI_ERR_CUDA, "batch_create: stream/event creation failed"));
+  *out = b;
+  return INFOLI_OK;
+}
+
+extern "C" int infoli_batch_set_stimulus_pulse(infoli_batch* b, int start_step, int end_step, float amp) {
+  infoli__clear_error();
+  if (!b) return infoli__fail(INFOLI_ERR_ARG, "null handle");
+  b->pulse_start = start_step;
+  b->pulse_end = end_step;
+  b->pulse_amp = amp;
+  b->graph_steps = -1;  // the captured graph holds the old schedule
+  return INFOLI_OK;
+}
+
+extern "C" int infoli_batch_run(infoli_batch* b, int n_steps) {
+  infoli__clear_error();
+  if (!b || n_steps < 0) return infoli__fail(INFOLI_ERR_ARG, "batch_run: bad argument");
+  BK(cudaSetDevice(b->device));
+  if (b->graph_steps != n_steps) {
+    // capture the group launches + the step advance once per run length
+    if (b->graph_exec) cudaGraphExecDestroy(b->graph_exec);
+    if (b->graph) cudaGraphDestroy(b->graph);
+    b->graph_exec = nullptr;
+    b->graph = nullptr;
+    BatchArgs a{};
+    a.P = b->P;
+    a.cta = b->d_cta;
+    a.bits = b->d_bits;
+    a.st = b->d_st;
+    a.ca = b->d_ca;
+    a.total = b->total;
+    a.step = b->d_step;
+    a.n_steps = n_steps;
+    a.pulse_start = b->pulse_start;
+    a.pulse_end = b->pulse_end;
+    a.pulse_amp = b->pulse_amp;
+    a.cta_ns = b->d_cta_ns;
+    BK(cudaStreamBeginCapture(b->stream, cudaStreamCaptureModeThreadLocal));
+    cudaError_t e = cudaEventRecord(b->fork, b->stream);
+    for (const BatchGroup& g : b->groups) {
+      if (e == cudaSuccess) e = cudaStreamWaitEvent(g.stream, b->fork, 0);
+      if (e == cudaSuccess) e = launch_group(b, g, a);
+      if (e == cudaSuccess) e = cudaEventRecord(g.done, g.stream);
+      if (e == cudaSuccess) e = cudaStreamWaitEvent(b->stream, g.done, 0);
+    }
+    if (e == cudaSuccess) {
+      batch_advance<<<1, 32, 0, b->stream>>>(b->d_step, n_steps);
+      e = cudaGetLastError();
+    }
+    cudaError_t e3 = cudaStreamEndCapture(b->stream, &b->graph);
+    if (e != cudaSuccess || e3 != cudaSuccess)
+      return infoli__fail(INFOLI_ERR_CUDA, "batch_run: capture failed: %s / %s", cudaGetErrorString(e),
+                          cudaGetErrorString(e3));
+    BK(cudaGraphInstantiate(&b->graph_exec, b->graph, 0));
+    b->graph_steps = n_steps;
+  }
+  BK(cudaEventRecord(b->ev0, b->stream));
+  BK(cudaGraphLaunch(b->graph_exec, b->stream));
+  BK(cudaEventRecord(b->ev1, b->stream));
+  BK(cudaStreamSynchronize(b->stream));
+  BK(cudaEventElapsedTime(&b->last_ms, b->ev0, b->ev1));
+  return INFOLI_OK;
+}
+
+extern "C" int infoli_batch_get_state(infoli_batch* b, float* out) {
+  infoli__clear_error();
+  if (!b || !out) return infoli__fail(INFOLI_ERR_ARG, "batch_get_state: bad argument");
+  BK(cudaSetDevice(b->device));
+  BK(cudaStreamSynchronize(b->stream));
+  BK(cudaMemcpy(out, b->d_st, sizeof(float) * (size_t)INFOLI_NSTATE * b->total, cudaMemcpyDeviceToHost));
+  std::vector<double> ca((size_t)b->total);
+  BK(cudaMemcpy(ca.data(), b->d_ca, sizeof(double) * ca.size(), cudaMemcpyDeviceToHost));
+  for (long long i = 0; i < b->total; ++i) out[4 * b->total + i] = (float)ca[(size_t)i];
+  return INFOLI_OK;
+}
+
+extern "C" int infoli_batch_set_state(infoli_batch* b, const float* in) {
+  infoli__clear_error();
+  if (!b || !in) return infoli__fail(INFOLI_ERR_ARG, "batch_set_state: bad argument");
+  BK(cudaSetDevice(b->device));
+  BK(cudaStreamSynchronize(b->stream));
+  BK(cudaMemcpy(b->d_st, in, sizeof(float) * (size_t)INFOLI_NSTATE * b->total, cudaMemcpyHostToDevice));
+  std::vector<double> ca(in + 4 * b->total, in + 5 * b->total);
+  BK(cudaMemcpy(b->d_ca, ca.data(), sizeof(double) * ca.size(), cudaMemcpyHostToDevice));
+  return INFOLI_OK;
+}
+
+extern "C" int infoli_batch_info(infoli_batch* b, int* ctas, int* cluster, int* block, int64_t* cells,
+                                 float* last_ms) {
+  infoli__clear_error();
+  if (!b) return infoli__fail(INFOLI_ERR_ARG, "null handle");
+  int cs = 1;
+  for (const BatchGroup& g : b->groups) cs = std::max(cs, g.cs);
+  if (ctas) *ctas = (int)b->cta.size();
+  if (cluster) *cluster = cs;
+  if (block) *block = b->block;
+  if (cells) *cells = b->total;
+  if (last_ms) *last_ms = b->last_ms;
+  return INFOLI_OK;
+}
+
+extern "C" int infoli_batch_cta_info(infoli_batch* b, int* max_active_clusters, int32_t* net, int64_t* start_ns,
+                                     int64_t* end_ns) {
+  infoli__clear_error();
+  if (!b) return infoli__fail(INFOLI_ERR_ARG, "null handle");
+  if (max_active_clusters) *max_active_clusters = b->groups.empty() ? 0 : b->groups.front().max_active;
+  for (size_t i = 0; i < b->cta.size(); ++i)
+    if (net) net[i] = b->cta[i].net;
+  if (start_ns || end_ns) {
+    BK(cudaSetDevice(b->device));
+    BK(cudaStreamSynchronize(b->stream));
+    std::vector<unsigned long long> t(2 * b->cta.size());
+    BK(cudaMemcpy(t.data(), b->d_cta_ns, sizeof(unsigned long long) * t.size(), cudaMemcpyDeviceToHost));
+    unsigned long long t0 = ~0ull;
+    for (size_t i = 0; i < b->cta.size(); ++i) t0 = std::min(t0, t[2 * i]);
+    for (size_t i = 0; i < b->cta.size(); ++i) {
+      if (start_ns) start_ns[i] = (int64_t)(t[2 * i] - t0);
+      if (end_ns) end_ns[i] = (int64_t)(t[2 * i + 1] - t0);
+    }
+  }
+  return INFOLI_OK;
+}
+
+extern "C" int infoli_batch_destroy(infoli_batch* b) {
+  infoli__clear_error();
+  batch_release(b);
+  return INFOLI_OK;
+}

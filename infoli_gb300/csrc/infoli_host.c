@@ -234,3 +234,26 @@ int infoli_bitmask_to_csr(int n, const uint32_t* bits, int64_t* row_ptr, int32_t
                                    (long long)e, (long long)cap);
   return INFOLI_OK;
 }
+
+/* Receiver r draws from its own splitmix64 stream, one draw per sender in
+ * ascending order (self skipped), so rows are independent of each other and
+ * of the thread that makes them. */
+int infoli_gen_bitmask(int n, float p, uint64_t seed, uint32_t* bits) {
+  infoli__clear_error();
+  if (n <= 0 || !bits || !(p >= 0.0f)) return infoli__fail(INFOLI_ERR_ARG, "gen_bitmask: bad argument");
+  const int64_t words = (n + 31) / 32;
+  const double pt = (double)p * 16777216.0;
+  const uint32_t thr = pt >= 16777216.0 ? 16777216u : (uint32_t)pt;
+#pragma omp parallel for schedule(dynamic, 16)
+  for (int r = 0; r < n; r++) {
+    uint64_t st = seed + (uint64_t)(r + 1) * 0x632BE59BD9B4E019ull;
+    uint32_t* row = bits + (int64_t)r * words;
+    for (int64_t w = 0; w < words; w++) row[w] = 0;
+    for (int s = 0; s < n; s++) {
+      if (s == r) continue;
+      const uint32_t u = (uint32_t)(sm64_next(&st) >> 40);
+      if (u < thr) row[s >> 5] |= 1u << (s & 31);
+    }
+  }
+  return INFOLI_OK;
+}
