@@ -508,17 +508,137 @@ def run_reference_batched(args, world, rank):
     return 0
 
 
+# ---------------------------------------------------------------- serving --
+SERVE_RATE, SERVE_REQUESTS = 50.0, 24
+
+
+def serving_requests(conf, count, seed=SEED):
+    """Poisson arrivals (mean SERVE_RATE per s); sizes log-uniform 500-50,000
+    cells; durations U(100, 2000) ms = 2,000-40,000 steps of 0.05 ms; density
+    U(0.01, 0.30); g = 0.04; topology from seed 1000 + k."""
+    import numpy as np
+
+    import infoli_gb300 as ig
+    from infoli_gb300 import workloads
+
+    rng = np.random.default_rng(seed)
+    t = np.cumsum(rng.exponential(1.0 / SERVE_RATE, count))
+    t -= t[0]
+    sizes = np.exp(rng.uniform(np.log(500), np.log(50000), count)).astype(np.int64)
+    steps = np.round(rng.uniform(100, 2000, count) / 0.05).astype(np.int64)
+    dens = rng.uniform(0.01, 0.30, count)
+    reqs = []
+    for k in range(count):
+        n = int(sizes[k])
+        rp, col = ig.gen_bitmask_csr(n, float(dens[k]), 1000 + k)
+        reqs.append(dict(n=n, row_ptr=rp, col=col, n_steps=int(steps[k]), g_uniform=0.04,
+                         init_state=workloads.perturbed_state(conf, n, rng)))
+    return t, reqs
+
+
+def run_gpu_serving(args, world, rank, local):
+    import numpy as np
+    import torch
+
+    import infoli_gb300 as ig
+    from infoli_gb300 import build
+
+    torch.cuda.set_device(local)
+    build.build()
+    conf = ig.read_parameters(os.path.join(ROOT, "infoli_gb300", "host", "default.conf"))
+    count = args.steps
+    arrivals, reqs = serving_requests(conf, count)
+    work = np.array([len(r["col"]) * r["n_steps"] for r in reqs], dtype=np.float64)
+    with ig.Server(conf, device=local, kahan=True) as sv:
+        # warm-up: small requests through the same server
+        wu = [sv.submit(n=r["n"], row_ptr=r["row_ptr"], col=r["col"], n_steps=200, g_uniform=0.04,
+                        init_state=r["init_state"]) for r in sorted(reqs, key=lambda r: r["n"])[:args.warmup]]
+        for i in wu:
+            sv.wait(i, want_state=False)
+        dist_barrier(world)
+        t0 = time.perf_counter()
+        ids = []
+        with ClockSampler(local) as clk:
+            for k, r in enumerate(reqs):
+                delay = arrivals[k] - (time.perf_counter() - t0)
+                if delay > 0:
+                    time.sleep(delay)
+                ids.append((sv.submit(**r), time.perf_counter() - t0))
+            infos = [sv.wait(i, want_state=False)[1] for i, _ in ids]
+        makespan = time.perf_counter() - t0
+    lat = np.array([i["done_s"] - i["submit_s"] for i in infos])
+    served = count / makespan
+
+    # sequential plain runs: each request alone through infoli_sim (create +
+    # run + state read back, the whole GPU), then a first-in-first-out
+    # schedule with the same arrival times
+    service = []
+    for r in reqs:
+        ts = time.perf_counter()
+        with ig.Simulation(r["n"], conf, r["row_ptr"], r["col"], g_uniform=0.04, init_state=r["init_state"],
+                           kahan=True, device=local) as sim:
+            sim.run(r["n_steps"])
+            sim.get_state()
+        service.append(time.perf_counter() - ts)
+    finish, seq_lat = 0.0, []
+    for a, sdur in zip(arrivals, service):
+        finish = max(finish, a) + sdur
+        seq_lat.append(finish - a)
+    seq_lat = np.array(seq_lat)
+    seq_rate = count / finish
+
+    result = None
+    if rank == 0:
+        in_bytes = sum(r["row_ptr"].nbytes + r["col"].nbytes + r["init_state"].nbytes for r in reqs)
+        result = {
+            "metric": "served sims/s", "value": served, "unit": "sims/s", "n_gpus": world, "steps": count,
+            "warmup": args.warmup, "ms_per_step": 1e3 * makespan / count, "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
+            "config": {"workload": f"Poisson request stream, mean {SERVE_RATE:g}/s, {count} requests (one per "
+                                   f"bench step), sizes log-uniform 500-50000 cells, durations U(100,2000) ms, "
+                                   f"density U(0.01,0.30), g=0.04, admitted by HBM budget (80% of free memory)",
+                       "requests": count, "cells": [r["n"] for r in reqs], "steps": [r["n_steps"] for r in reqs],
+                       "edges": [int(len(r["col"])) for r in reqs], "timing": "host wall clock from the first "
+                       "arrival to the last result (serving is end to end)", "l2": "inputs larger than L2"},
+            "latency_s": {"p50": float(np.percentile(lat, 50)), "p99": float(np.percentile(lat, 99)),
+                          "max": float(lat.max())},
+            "sequential_plain": {"value": seq_rate, "unit": "sims/s",
+                                 "latency_s": {"p50": float(np.percentile(seq_lat, 50)),
+                                               "p99": float(np.percentile(seq_lat, 99))},
+                                 "sample": "every request alone through infoli_sim (create+run+read), FIFO "
+                                           "schedule on the same arrivals"},
+            "offered_edge_evals_per_s": float(work.sum() / max(arrivals[-1], 1e-9)),
+            "sustained_edge_evals_per_s": float(work.sum() / makespan),
+            "e2e": {"value": served, "unit": "sims/s", "h2d_bytes_per_step": int(in_bytes / count),
+                    "d2h_bytes_per_step": int(sum(19 * 4 * r["n"] for r in reqs) / count)},
+            "grid_per_request": [i["grid"] for i in infos],
+            "prepare_s_per_request": [round(i["prepared_s"] - i["admit_s"], 3) for i in infos],
+            "run_s_per_request": [round(i["done_s"] - i["start_s"], 3) for i in infos],
+            "plain_service_s_per_request": [round(x, 3) for x in service],
+            "gpu_launches": int(sum((r["n_steps"] + 8191) // 8192 for r in reqs)),
+            "clocks": clk.summary(),
+        }
+        print(json.dumps(result))
+    return 0
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
     ap.add_argument("--steps", type=int, default=None)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
-    ap.add_argument("--workload", default="grid10k", choices=["grid10k", "batched"])
+    ap.add_argument("--workload", default="grid10k", choices=["grid10k", "batched", "serving"])
     args = ap.parse_args()
     if args.steps is None:
-        args.steps = 40 if args.workload == "grid10k" else 10
+        args.steps = {"grid10k": 40, "batched": 10, "serving": SERVE_REQUESTS}[args.workload]
     world, rank, local = dist_setup()
+    if args.workload == "serving":
+        if args.impl == "reference":
+            print(json.dumps({"impl": "reference", "unavailable": "the reference has no serving mode; its "
+                              "per-request CPU cost is the grid10k reference arm"}))
+            return 0
+        return run_gpu_serving(args, world, rank, local)
     if args.workload == "batched":
         if args.impl == "reference":
             return run_reference_batched(args, world, rank)

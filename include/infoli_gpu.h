@@ -139,6 +139,10 @@ int infoli_bitmask_to_csr(int n, const uint32_t* bits, int64_t* row_ptr, int32_t
  * one draw per sender in ascending order, so rows are generated in parallel
  * and the result does not depend on the thread count. */
 int infoli_gen_bitmask(int n, float p, uint64_t seed, uint32_t* bits);
+/* The same matrix in CSR form (infoli_gen_uniform's output contract),
+ * generated without the bitmask. */
+int infoli_gen_bitmask_csr(int n, float p, uint64_t seed, int64_t* row_ptr, int32_t* col, int64_t cap,
+                           int64_t* n_edges);
 
 /* ------------------------------------------------------------------------ */
 /* one simulation on the GPU                                                */
@@ -160,6 +164,7 @@ typedef struct {
   float g_uniform;           /* conductance of every edge when g is NULL (CONDUCTANCE) */
   int flags;                 /* INFOLI_F_* */
   int device;                /* CUDA device ordinal */
+  int grid;                  /* CTAs (one per SM) the simulation may use; 0 = all SMs */
 } infoli_sim_desc;
 
 /* Trace callback: called once per recorded step with the values of that step
@@ -222,6 +227,20 @@ int infoli_sim_get_profile(infoli_sim* s, double mean_ns[5], double max_ns[5]);
 
 int infoli_sim_destroy(infoli_sim* s);
 
+/* Asynchronous form of a run without trace (no counterpart in the
+ * reference): enqueues n_steps steps on the simulation's own CUDA stream and
+ * returns at once; the step counter advances immediately.  Simulations with
+ * distinct handles run concurrently on the GPU when their grids fit side by
+ * side.  infoli_sim_query returns 1 when all enqueued work has finished (0
+ * while it runs, a negative status on a device error); infoli_sim_sync waits
+ * for it.  get_state / set_state / run wait for enqueued work first. */
+int infoli_sim_launch(infoli_sim* s, int n_steps);
+/* Device memory the handle holds for its plan and state (bytes; trace
+ * buffers and profiling timers excluded). */
+int infoli_sim_memory(infoli_sim* s, int64_t* device_bytes);
+int infoli_sim_query(infoli_sim* s);
+int infoli_sim_sync(infoli_sim* s);
+
 /* ------------------------------------------------------------------------ */
 /* many independent networks in one launch                                   */
 /* ------------------------------------------------------------------------ */
@@ -273,6 +292,68 @@ int infoli_batch_info(infoli_batch* b, int* ctas, int* cluster, int* block, int6
 int infoli_batch_cta_info(infoli_batch* b, int* max_active_clusters, int32_t* net, int64_t* start_ns,
                           int64_t* end_ns);
 int infoli_batch_destroy(infoli_batch* b);
+
+/* ------------------------------------------------------------------------ */
+/* serving: a request loop over many simulations                             */
+/* ------------------------------------------------------------------------ */
+
+/* No counterpart in the reference (one network per process).  A server
+ * admits simulation requests by device-memory budget, builds each one's plan
+ * on a pool of host threads, runs admitted requests side by side on the GPU
+ * (each on its own stream and its own share of the SMs, chosen from its size)
+ * and keeps their state on the device until they finish.  Requests that
+ * arrive while others run start as soon as memory and SMs free up.  A
+ * request's result does not depend on the other requests. */
+typedef struct infoli_server infoli_server;
+
+typedef struct {
+  const float* params;   /* [INFOLI_NPARAM] shared by all requests */
+  int device;
+  int64_t hbm_budget;    /* device bytes admitted requests may hold; 0 = 80% of free memory */
+  int max_active;        /* requests admitted at once (preparing or running); 0 = 16 */
+  int64_t work_per_cta;  /* edge evaluations per step per CTA when sizing a request's SM share; 0 = 262144 */
+  int backfill_ms;       /* later requests may pass a head request that does not fit yet for this long; 0 = 1000 */
+  int prep_threads;      /* host threads building plans; 0 = 4 */
+  int flags;             /* INFOLI_F_KAHAN for every request */
+} infoli_server_desc;
+
+typedef struct {
+  int n_cells;
+  const int64_t* row_ptr;     /* CSR by receiver, as infoli_sim_desc */
+  const int32_t* col;
+  const float* g;             /* per-edge conductance or NULL */
+  float g_uniform;
+  const float* init_state;    /* [INFOLI_NSTATE * n_cells] or NULL */
+  const float* init_values;   /* [INFOLI_NSTATE] when init_state is NULL */
+  int n_steps;                /* simulated steps */
+  int pulse_start, pulse_end; /* dendritic pulse of pulse_amp for pulse_start <= step < pulse_end */
+  float pulse_amp;
+} infoli_request_desc;
+
+typedef struct {
+  int64_t id;
+  int n_cells, n_steps;
+  int grid;                   /* CTAs (SMs) it ran on */
+  int64_t device_bytes;       /* device memory it held */
+  int64_t admitted_bytes;     /* budget reserved at admission (an estimate made before planning) */
+  /* seconds since the server was created: submitted, admitted, plan and
+   * upload done, launched, finished */
+  double submit_s, admit_s, prepared_s, start_s, done_s;
+  int status;                 /* INFOLI_OK or the request's error */
+} infoli_request_info;
+
+int infoli_server_create(const infoli_server_desc* desc, infoli_server** out);
+/* Copies the request's inputs and queues it; returns at once with its id.
+ * INFOLI_ERR_CAPACITY when the request alone exceeds the budget. */
+int infoli_server_submit(infoli_server* sv, const infoli_request_desc* req, int64_t* id);
+/* 0 queued, 1 admitted or running, 2 finished. */
+int infoli_server_poll(infoli_server* sv, int64_t id);
+/* Waits for the request, copies its final state ([INFOLI_NSTATE * n_cells],
+ * may be NULL) and timing, and forgets the id.  Returns the request's status. */
+int infoli_server_wait(infoli_server* sv, int64_t id, float* out_state, infoli_request_info* info);
+int infoli_server_status(infoli_server* sv, int* queued, int* active, int64_t* completed, int64_t* hbm_in_use);
+/* Waits for running requests and drops queued ones. */
+int infoli_server_destroy(infoli_server* sv);
 
 /* ------------------------------------------------------------------------ */
 /* allocation-free run                                                       */

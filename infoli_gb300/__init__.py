@@ -6,13 +6,13 @@ it (build); there is no CPU implementation of the step here.
 """
 from . import capi  # noqa: F401
 from .capi import (  # noqa: F401
-    Batch, InfoliError, Simulation, S, STATE_NAMES, TRACE_AXON, TRACE_DEND, TRACE_SOMA, bitmask_to_csr,
-    device_count, format_f8, format_row, gen_bitmask, gen_fixed_degree, gen_grid_gaussian, gen_uniform,
+    Batch, InfoliError, Server, Simulation, S, STATE_NAMES, TRACE_AXON, TRACE_DEND, TRACE_SOMA, bitmask_to_csr,
+    device_count, format_f8, format_row, gen_bitmask, gen_bitmask_csr, gen_fixed_degree, gen_grid_gaussian, gen_uniform,
     read_gcal, read_parameters,
 )
 
 __all__ = [
-    "capi", "Batch", "InfoliError", "Simulation", "gen_bitmask", "S", "STATE_NAMES", "TRACE_AXON", "TRACE_SOMA",
+    "capi", "Batch", "InfoliError", "Server", "Simulation", "gen_bitmask", "gen_bitmask_csr", "S", "STATE_NAMES", "TRACE_AXON", "TRACE_SOMA",
     "TRACE_DEND", "bitmask_to_csr", "device_count", "format_f8", "format_row", "gen_fixed_degree",
     "gen_grid_gaussian", "gen_uniform", "read_gcal", "read_parameters",
 ]

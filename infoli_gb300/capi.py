@@ -41,10 +41,12 @@ EXPORTED = [
     "infoli_sim_run_into", "infoli_sim_get_state", "infoli_sim_set_state", "infoli_sim_step",
     "infoli_sim_last_run_stats", "infoli_sim_plan_info", "infoli_sim_destroy", "infoli_format_f8",
     "infoli_format_row", "infoli_sim_set_profiling", "infoli_sim_get_profile", "infoli_plan_emulate",
-    "infoli_run_noalloc", "infoli_gen_bitmask", "infoli_batch_create", "infoli_batch_set_stimulus_pulse",
+    "infoli_run_noalloc", "infoli_sim_launch", "infoli_sim_query", "infoli_sim_sync",
+    "infoli_sim_memory", "infoli_gen_bitmask_csr", "infoli_gen_bitmask", "infoli_batch_create", "infoli_batch_set_stimulus_pulse",
     "infoli_batch_run", "infoli_batch_get_state", "infoli_batch_set_state", "infoli_batch_info",
     "infoli_batch_cta_info",
-    "infoli_batch_destroy",
+    "infoli_batch_destroy", "infoli_server_create", "infoli_server_submit", "infoli_server_poll",
+    "infoli_server_wait", "infoli_server_status", "infoli_server_destroy",
 ]
 
 
@@ -66,6 +68,7 @@ class SimDesc(C.Structure):
         ("g_uniform", C.c_float),
         ("flags", C.c_int),
         ("device", C.c_int),
+        ("grid", C.c_int),
     ]
 
 
@@ -80,6 +83,52 @@ class BatchDesc(C.Structure):
         ("g", C.c_void_p),
         ("flags", C.c_int),
         ("device", C.c_int),
+    ]
+
+
+class ServerDesc(C.Structure):
+    _fields_ = [
+        ("params", C.c_void_p),
+        ("device", C.c_int),
+        ("hbm_budget", C.c_int64),
+        ("max_active", C.c_int),
+        ("work_per_cta", C.c_int64),
+        ("backfill_ms", C.c_int),
+        ("prep_threads", C.c_int),
+        ("flags", C.c_int),
+    ]
+
+
+class RequestDesc(C.Structure):
+    _fields_ = [
+        ("n_cells", C.c_int),
+        ("row_ptr", C.c_void_p),
+        ("col", C.c_void_p),
+        ("g", C.c_void_p),
+        ("g_uniform", C.c_float),
+        ("init_state", C.c_void_p),
+        ("init_values", C.c_void_p),
+        ("n_steps", C.c_int),
+        ("pulse_start", C.c_int),
+        ("pulse_end", C.c_int),
+        ("pulse_amp", C.c_float),
+    ]
+
+
+class RequestInfo(C.Structure):
+    _fields_ = [
+        ("id", C.c_int64),
+        ("n_cells", C.c_int),
+        ("n_steps", C.c_int),
+        ("grid", C.c_int),
+        ("device_bytes", C.c_int64),
+        ("admitted_bytes", C.c_int64),
+        ("submit_s", C.c_double),
+        ("admit_s", C.c_double),
+        ("prepared_s", C.c_double),
+        ("start_s", C.c_double),
+        ("done_s", C.c_double),
+        ("status", C.c_int),
     ]
 
 
@@ -119,11 +168,16 @@ def load():
         "infoli_sim_last_run_stats": ([P, P, P], I),
         "infoli_sim_plan_info": ([P, P, P, P, P, P], I),
         "infoli_sim_destroy": ([P], I),
+        "infoli_sim_launch": ([P, I], I),
+        "infoli_sim_query": ([P], I),
+        "infoli_sim_sync": ([P], I),
+        "infoli_sim_memory": ([P, P], I),
         "infoli_plan_emulate": ([I, P, P, P, F, I, I, I, I64, I, P, P, P], I),
         "infoli_run_noalloc": ([P, I, P, P, P, F, I, I, F, P, I, I, P, P], I),
         "infoli_sim_set_profiling": ([P, I], I),
         "infoli_sim_get_profile": ([P, P, P], I),
         "infoli_gen_bitmask": ([I, F, C.c_uint64, P], I),
+        "infoli_gen_bitmask_csr": ([I, F, C.c_uint64, P, P, I64, P], I),
         "infoli_batch_create": ([C.POINTER(BatchDesc), C.POINTER(C.c_void_p)], I),
         "infoli_batch_set_stimulus_pulse": ([P, I, I, F], I),
         "infoli_batch_run": ([P, I], I),
@@ -132,6 +186,12 @@ def load():
         "infoli_batch_info": ([P, P, P, P, P, P], I),
         "infoli_batch_cta_info": ([P, P, P, P, P], I),
         "infoli_batch_destroy": ([P], I),
+        "infoli_server_create": ([C.POINTER(ServerDesc), C.POINTER(C.c_void_p)], I),
+        "infoli_server_submit": ([P, C.POINTER(RequestDesc), P], I),
+        "infoli_server_poll": ([P, I64], I),
+        "infoli_server_wait": ([P, I64, P, C.POINTER(RequestInfo)], I),
+        "infoli_server_status": ([P, P, P, P, P], I),
+        "infoli_server_destroy": ([P], I),
         "infoli_format_f8": ([C.c_char_p, F], I),
         "infoli_format_row": ([C.c_char_p, I64, P, I, I, I], I64),
     }
@@ -255,7 +315,7 @@ class Simulation:
     """One network on the GPU (infoli_sim_* handle)."""
 
     def __init__(self, n, params, row_ptr, col, g=None, g_uniform=None, init_state=None,
-                 init_values=None, kahan=False, device=0):
+                 init_values=None, kahan=False, device=0, grid=0):
         L = load()
         self._L = L
         params = np.ascontiguousarray(params, dtype=np.float32)
@@ -283,6 +343,7 @@ class Simulation:
         d.g_uniform = float(self.params[1] if g_uniform is None else g_uniform)
         d.flags = F_KAHAN if kahan else 0
         d.device = int(device)
+        d.grid = int(grid)
         h = C.c_void_p()
         _check(L.infoli_sim_create(C.byref(d), C.byref(h)))
         self._h = h
@@ -331,6 +392,21 @@ class Simulation:
         assert got.value == rows
         return {nm: out[:rows, i, :].copy() for i, nm in enumerate(names)}
 
+    def launch(self, n_steps):
+        """Enqueue n_steps (no trace) and return at once."""
+        _check(self._L.infoli_sim_launch(self._h, int(n_steps)))
+
+    def query(self) -> bool:
+        return bool(_check(self._L.infoli_sim_query(self._h)))
+
+    def sync(self):
+        _check(self._L.infoli_sim_sync(self._h))
+
+    def device_bytes(self) -> int:
+        v = C.c_int64()
+        _check(self._L.infoli_sim_memory(self._h, C.byref(v)))
+        return v.value
+
     def run_with_callback(self, n_steps, trace_every, what, fn):
         """fn(step, what_bit, values[n]) per recorded quantity, in step order."""
         def _cb(user, step, w, values, n):
@@ -378,6 +454,13 @@ def gen_bitmask(n: int, p: float, seed: int) -> np.ndarray:
     bits = np.zeros((n, (n + 31) // 32), dtype=np.uint32)
     _check(load().infoli_gen_bitmask(int(n), float(p), int(seed) & (2**64 - 1), _p(bits)))
     return bits
+
+
+def gen_bitmask_csr(n: int, p: float, seed: int):
+    """CSR of gen_bitmask(n, p, seed) (include/infoli_gpu.h: infoli_gen_bitmask_csr)."""
+    L = load()
+    return _csr_call(L.infoli_gen_bitmask_csr, n, n, float(p), int(seed) & (2**64 - 1),
+                     cap_hint=n * (n - 1) * min(1.0, float(p) * 1.05 + 0.002) + 1024)
 
 
 class Batch:
@@ -466,3 +549,80 @@ class Batch:
         t1 = np.zeros(k, np.int64)
         _check(self._L.infoli_batch_cta_info(self._h, C.byref(mac), _p(net), _p(t0), _p(t1)))
         return {"max_active_clusters": mac.value, "net": net, "start_ns": t0, "end_ns": t1}
+
+
+class Server:
+    """Request loop over many simulations on one GPU (infoli_server_* handle)."""
+
+    def __init__(self, params, device=0, hbm_budget=0, max_active=0, work_per_cta=0, backfill_ms=0,
+                 prep_threads=0, kahan=False):
+        L = load()
+        self._L = L
+        self.params = np.ascontiguousarray(params, dtype=np.float32)[:NPARAM].copy()
+        d = ServerDesc()
+        d.params = _p(self.params)
+        d.device = int(device)
+        d.hbm_budget = int(hbm_budget)
+        d.max_active = int(max_active)
+        d.work_per_cta = int(work_per_cta)
+        d.backfill_ms = int(backfill_ms)
+        d.prep_threads = int(prep_threads)
+        d.flags = F_KAHAN if kahan else 0
+        h = C.c_void_p()
+        _check(L.infoli_server_create(C.byref(d), C.byref(h)))
+        self._h = h
+        self._n = {}
+
+    def close(self):
+        if getattr(self, "_h", None):
+            self._L.infoli_server_destroy(self._h)
+            self._h = None
+
+    __del__ = close
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *exc):
+        self.close()
+
+    def submit(self, n, row_ptr, col, n_steps, g=None, g_uniform=0.04, init_state=None, init_values=None,
+               pulse=(20000, 20499, 6.0)) -> int:
+        rp = np.ascontiguousarray(row_ptr, dtype=np.int64)
+        cl = np.ascontiguousarray(col, dtype=np.int32)
+        gg = None if g is None else np.ascontiguousarray(g, dtype=np.float32)
+        q = RequestDesc()
+        q.n_cells = int(n)
+        q.row_ptr = _p(rp)
+        q.col = _p(cl) if cl.size else None
+        q.g = _p(gg)
+        q.g_uniform = float(g_uniform)
+        if init_state is not None:
+            st = np.ascontiguousarray(init_state, dtype=np.float32).reshape(NSTATE, int(n))
+            q.init_state = _p(st)
+        else:
+            iv = np.ascontiguousarray(init_values, dtype=np.float32)
+            q.init_values = _p(iv)
+        q.n_steps = int(n_steps)
+        q.pulse_start, q.pulse_end, q.pulse_amp = int(pulse[0]), int(pulse[1]), float(pulse[2])
+        rid = C.c_int64()
+        _check(self._L.infoli_server_submit(self._h, C.byref(q), C.byref(rid)))
+        self._n[rid.value] = int(n)
+        return rid.value
+
+    def poll(self, rid) -> int:
+        return _check(self._L.infoli_server_poll(self._h, int(rid)))
+
+    def wait(self, rid, want_state=True):
+        """Returns (state [19, n] or None, info dict)."""
+        n = self._n.pop(int(rid))
+        out = np.zeros((NSTATE, n), dtype=np.float32) if want_state else None
+        info = RequestInfo()
+        _check(self._L.infoli_server_wait(self._h, int(rid), _p(out), C.byref(info)))
+        return out, {k: getattr(info, k) for k, _ in RequestInfo._fields_}
+
+    def status(self):
+        q, a = C.c_int(), C.c_int()
+        c, m = C.c_int64(), C.c_int64()
+        _check(self._L.infoli_server_status(self._h, C.byref(q), C.byref(a), C.byref(c), C.byref(m)))
+        return {"queued": q.value, "active": a.value, "completed": c.value, "hbm_in_use": m.value}

@@ -4,9 +4,11 @@
 #include <cuda_runtime.h>
 
 #include <algorithm>
+#include <cstdint>
 #include <cstdio>
 #include <cstdlib>
 #include <cstring>
+#include <mutex>
 #include <string>
 #include <vector>
 
@@ -38,12 +40,45 @@ unsigned long long wait_timeout_ns() {
   return (unsigned long long)ms * 1000000ull;
 }
 
+// Device memory of simulation handles comes from one stream-ordered pool per
+// device (cudaMallocFromPoolAsync / cudaFreeAsync on the handle's stream).
+// Plain cudaMalloc / cudaFree synchronise with work already running on the
+// device, so creating or destroying one handle would stall the kernels of
+// every other handle; stream-ordered allocation does not.  Freed memory stays
+// in the pool for the next handle (release threshold: unlimited).
+cudaMemPool_t sim_pool(int device) {
+  static std::mutex mu;
+  static cudaMemPool_t pools[64] = {};
+  std::lock_guard<std::mutex> lk(mu);
+  if (device < 0 || device >= 64) return nullptr;
+  if (!pools[device]) {
+    cudaMemPoolProps props = {};
+    props.allocType = cudaMemAllocationTypePinned;
+    props.location.type = cudaMemLocationTypeDevice;
+    props.location.id = device;
+    if (cudaMemPoolCreate(&pools[device], &props) != cudaSuccess) {
+      pools[device] = nullptr;
+      return nullptr;
+    }
+    uint64_t keep = UINT64_MAX;
+    cudaMemPoolSetAttribute(pools[device], cudaMemPoolAttrReleaseThreshold, &keep);
+  }
+  return pools[device];
+}
+
 template <class T>
-int dev_upload(T** dst, const T* src, size_t count) {
+cudaError_t pool_alloc(T** dst, size_t bytes, int device, cudaStream_t st) {
+  cudaMemPool_t pool = sim_pool(device);
+  if (!pool) return cudaErrorMemoryAllocation;
+  return cudaMallocFromPoolAsync((void**)dst, bytes, pool, st);
+}
+
+template <class T>
+int dev_upload(T** dst, const T* src, size_t count, int device, cudaStream_t st) {
   *dst = nullptr;
   if (count == 0) return INFOLI_OK;
-  CK(cudaMalloc((void**)dst, count * sizeof(T)));
-  CK(cudaMemcpy(*dst, src, count * sizeof(T), cudaMemcpyHostToDevice));
+  CK(pool_alloc(dst, count * sizeof(T), device, st));
+  CK(cudaMemcpyAsync(*dst, src, count * sizeof(T), cudaMemcpyHostToDevice, st));
   return INFOLI_OK;
 }
 
@@ -92,6 +127,8 @@ struct infoli_sim {
   cudaEvent_t ev_t0 = nullptr, ev_t1 = nullptr;
   float last_ms = 0.0f;
   int last_launches = 0;
+  int async_pending = 0;  // infoli_sim_launch work not yet checked for device errors
+  int64_t dev_bytes = 0;  // device memory held for the plan and the state
 };
 
 namespace {
@@ -99,14 +136,16 @@ namespace {
 void release(infoli_sim* s) {
   if (!s) return;
   cudaSetDevice(s->device);
-  if (s->stream) cudaStreamSynchronize(s->stream);
   if (s->side) cudaStreamSynchronize(s->side);
   void* dptrs[] = {s->d_cta,   s->d_tiles,  s->d_chunks, s->d_cell_slots, s->d_edges,
                    s->d_edge_g, s->d_vd[0], s->d_vd[1],  s->d_st,         s->d_ca,
                    s->d_cell_amp, s->d_cell_onset, s->d_bar, s->d_err, s->d_trace[0], s->d_trace[1],
                    s->d_prof, s->d_probes, s->d_vll[0], s->d_vll[1], s->d_gdesc};
-  for (void* p : dptrs)
-    if (p) cudaFree(p);
+  if (s->stream) {
+    for (void* p : dptrs)
+      if (p) cudaFreeAsync(p, s->stream);
+    cudaStreamSynchronize(s->stream);
+  }
   for (float* h : s->h_trace)
     if (h) cudaFreeHost(h);
   for (cudaEvent_t e : {s->ev_kernel[0], s->ev_kernel[1], s->ev_copy[0], s->ev_copy[1], s->ev_t0, s->ev_t1})
@@ -137,10 +176,14 @@ int upload_state(infoli_sim* s, const float* state /*19 x n*/) {
     else
       std::copy(src, src + n, st.begin() + (size_t)f * np);
   }
-  CK(cudaMemcpy(s->d_st, st.data(), st.size() * sizeof(float), cudaMemcpyHostToDevice));
-  CK(cudaMemcpy(s->d_ca, ca.data(), ca.size() * sizeof(double), cudaMemcpyHostToDevice));
-  CK(cudaMemcpy(s->d_vd[s->step & 1], vd.data(), np * sizeof(float), cudaMemcpyHostToDevice));
-  CK(cudaMemcpy(s->d_vd[(s->step + 1) & 1], vd.data(), np * sizeof(float), cudaMemcpyHostToDevice));
+  // pageable sources: each call returns once its data is staged, so the
+  // local vectors may go out of scope
+  CK(cudaMemcpyAsync(s->d_st, st.data(), st.size() * sizeof(float), cudaMemcpyHostToDevice, s->stream));
+  CK(cudaMemcpyAsync(s->d_ca, ca.data(), ca.size() * sizeof(double), cudaMemcpyHostToDevice, s->stream));
+  CK(cudaMemcpyAsync(s->d_vd[s->step & 1], vd.data(), np * sizeof(float), cudaMemcpyHostToDevice, s->stream));
+  CK(cudaMemcpyAsync(s->d_vd[(s->step + 1) & 1], vd.data(), np * sizeof(float), cudaMemcpyHostToDevice,
+                     s->stream));
+  CK(cudaStreamSynchronize(s->stream));
   return INFOLI_OK;
 }
 
@@ -193,9 +236,10 @@ int nq_of(int what) { return !!(what & INFOLI_TRACE_AXON) + !!(what & INFOLI_TRA
 
 int check_device_error(infoli_sim* s) {
   int err = 0;
-  CK(cudaMemcpy(&err, s->d_err, sizeof(int), cudaMemcpyDeviceToHost));
+  CK(cudaMemcpyAsync(&err, s->d_err, sizeof(int), cudaMemcpyDeviceToHost, s->stream));
+  CK(cudaStreamSynchronize(s->stream));
   if (err != DEV_OK) {
-    cudaMemset(s->d_err, 0, sizeof(int));
+    cudaMemsetAsync(s->d_err, 0, sizeof(int), s->stream);
     return infoli__fail(INFOLI_ERR_TIMEOUT, "device wait gave up (code %d): %s", err,
                         err == DEV_ERR_BARRIER_TIMEOUT ? "grid barrier timeout"
                         : err == DEV_ERR_STAMP_TIMEOUT ? "stamped V_dend exchange timeout"
@@ -248,6 +292,9 @@ int infoli_sim_create(const infoli_sim_desc* d, infoli_sim** out) {
     return rc;
   };
   if (cudaSetDevice(s->device) != cudaSuccess) return fail(infoli__fail(INFOLI_ERR_CUDA, "cudaSetDevice failed"));
+  if (cudaStreamCreateWithFlags(&s->stream, cudaStreamNonBlocking) != cudaSuccess ||
+      cudaStreamCreateWithFlags(&s->side, cudaStreamNonBlocking) != cudaSuccess)
+    return fail(infoli__fail(INFOLI_ERR_CUDA, "stream creation failed"));
 
   // ---- plan
   int nsm = 0, smem_optin = 0;
@@ -262,6 +309,7 @@ int infoli_sim_create(const infoli_sim_desc* d, infoli_sim** out) {
   const char* gs = getenv("INFOLI_GRID");
   if (gs) pin.grid = atoi(gs);
   pin.grid_max = nsm;  // one CTA per SM
+  if (d->grid > 0) pin.grid_max = std::min(nsm, d->grid);  // a share of the SMs
   pin.smem_budget = (size_t)smem_optin - 1024;  // static shared (abort flag) headroom
   pin.kahan = s->kahan;
   pin.no_resident = getenv("INFOLI_NO_RESIDENT") ? 1 : 0;
@@ -288,37 +336,37 @@ int infoli_sim_create(const infoli_sim_desc* d, infoli_sim** out) {
     return fail(infoli__fail(INFOLI_ERR_CUDA, "plan needs %d co-resident CTAs, device allows %d", s->plan.grid, cores));
 
   int rc;
-  if ((rc = dev_upload(&s->d_cta, s->plan.cta.data(), s->plan.cta.size())) ||
-      (rc = dev_upload(&s->d_tiles, s->plan.tiles.data(), s->plan.tiles.size())) ||
-      (rc = dev_upload(&s->d_chunks, s->plan.chunks.data(), s->plan.chunks.size())) ||
-      (rc = dev_upload(&s->d_cell_slots, s->plan.cell_slots.data(), s->plan.cell_slots.size())) ||
-      (rc = dev_upload(&s->d_edges, s->plan.edges.data(), s->plan.edges.size())) ||
-      (rc = dev_upload(&s->d_edge_g, s->plan.edge_g.data(), s->plan.edge_g.size())) ||
-      (rc = dev_upload(&s->d_probes, s->plan.probes.data(), s->plan.probes.size())) ||
-      (rc = dev_upload(&s->d_gdesc, s->plan.gdesc.data(), s->plan.gdesc.size())))
+  const int dv = s->device;
+  cudaStream_t st0 = s->stream;
+  if ((rc = dev_upload(&s->d_cta, s->plan.cta.data(), s->plan.cta.size(), dv, st0)) ||
+      (rc = dev_upload(&s->d_tiles, s->plan.tiles.data(), s->plan.tiles.size(), dv, st0)) ||
+      (rc = dev_upload(&s->d_chunks, s->plan.chunks.data(), s->plan.chunks.size(), dv, st0)) ||
+      (rc = dev_upload(&s->d_cell_slots, s->plan.cell_slots.data(), s->plan.cell_slots.size(), dv, st0)) ||
+      (rc = dev_upload(&s->d_edges, s->plan.edges.data(), s->plan.edges.size(), dv, st0)) ||
+      (rc = dev_upload(&s->d_edge_g, s->plan.edge_g.data(), s->plan.edge_g.size(), dv, st0)) ||
+      (rc = dev_upload(&s->d_probes, s->plan.probes.data(), s->plan.probes.size(), dv, st0)) ||
+      (rc = dev_upload(&s->d_gdesc, s->plan.gdesc.data(), s->plan.gdesc.size(), dv, st0)))
     return fail(rc);
   // the kernel needs valid pointers even for empty tables
-  if (!s->d_chunks && cudaMalloc((void**)&s->d_chunks, sizeof(ChunkDesc)) != cudaSuccess)
-    return fail(infoli__fail(INFOLI_ERR_NOMEM, "cudaMalloc"));
-  if (!s->d_tiles && cudaMalloc((void**)&s->d_tiles, sizeof(TileDesc)) != cudaSuccess)
-    return fail(infoli__fail(INFOLI_ERR_NOMEM, "cudaMalloc"));
-  if (!s->d_edges && cudaMalloc((void**)&s->d_edges, 16) != cudaSuccess)
-    return fail(infoli__fail(INFOLI_ERR_NOMEM, "cudaMalloc"));
+  if ((!s->d_chunks && pool_alloc(&s->d_chunks, sizeof(ChunkDesc), dv, st0) != cudaSuccess) ||
+      (!s->d_tiles && pool_alloc(&s->d_tiles, sizeof(TileDesc), dv, st0) != cudaSuccess) ||
+      (!s->d_edges && pool_alloc(&s->d_edges, 16, dv, st0) != cudaSuccess))
+    return fail(infoli__fail(INFOLI_ERR_NOMEM, "sim_create: device allocation failed"));
 
   const size_t np = (size_t)s->n_pad;
-  if (cudaMalloc((void**)&s->d_vd[0], np * sizeof(float)) != cudaSuccess ||
-      cudaMalloc((void**)&s->d_vd[1], np * sizeof(float)) != cudaSuccess ||
-      cudaMalloc((void**)&s->d_st, (size_t)F_COUNT * np * sizeof(float)) != cudaSuccess ||
-      cudaMalloc((void**)&s->d_ca, np * sizeof(double)) != cudaSuccess ||
-      cudaMalloc((void**)&s->d_bar, 128) != cudaSuccess || cudaMalloc((void**)&s->d_err, 128) != cudaSuccess)
+  if (pool_alloc(&s->d_vd[0], np * sizeof(float), dv, st0) != cudaSuccess ||
+      pool_alloc(&s->d_vd[1], np * sizeof(float), dv, st0) != cudaSuccess ||
+      pool_alloc(&s->d_st, (size_t)F_COUNT * np * sizeof(float), dv, st0) != cudaSuccess ||
+      pool_alloc(&s->d_ca, np * sizeof(double), dv, st0) != cudaSuccess ||
+      pool_alloc(&s->d_bar, 128, dv, st0) != cudaSuccess || pool_alloc(&s->d_err, 128, dv, st0) != cudaSuccess)
     return fail(infoli__fail(INFOLI_ERR_NOMEM, "sim_create: device allocation failed"));
-  cudaMemset(s->d_vd[0], 0, np * sizeof(float));
-  cudaMemset(s->d_vd[1], 0, np * sizeof(float));
-  cudaMemset(s->d_err, 0, 128);
-  cudaMemset(s->d_bar, 0, 128);
+  cudaMemsetAsync(s->d_vd[0], 0, np * sizeof(float), st0);
+  cudaMemsetAsync(s->d_vd[1], 0, np * sizeof(float), st0);
+  cudaMemsetAsync(s->d_err, 0, 128, st0);
+  cudaMemsetAsync(s->d_bar, 0, 128, st0);
   if (s->plan.shape.stamped) {
-    if (cudaMalloc((void**)&s->d_vll[0], np * sizeof(unsigned long long)) != cudaSuccess ||
-        cudaMalloc((void**)&s->d_vll[1], np * sizeof(unsigned long long)) != cudaSuccess)
+    if (pool_alloc(&s->d_vll[0], np * sizeof(unsigned long long), dv, st0) != cudaSuccess ||
+        pool_alloc(&s->d_vll[1], np * sizeof(unsigned long long), dv, st0) != cudaSuccess)
       return fail(infoli__fail(INFOLI_ERR_NOMEM, "sim_create: device allocation failed"));
   }
 
@@ -331,17 +379,27 @@ int infoli_sim_create(const infoli_sim_desc* d, infoli_sim** out) {
     st = init.data();
   }
   if ((rc = upload_state(s, st))) return fail(rc);
-
-  if (cudaStreamCreateWithFlags(&s->stream, cudaStreamNonBlocking) != cudaSuccess ||
-      cudaStreamCreateWithFlags(&s->side, cudaStreamNonBlocking) != cudaSuccess)
-    return fail(infoli__fail(INFOLI_ERR_CUDA, "stream creation failed"));
   for (int i = 0; i < 2; ++i)
     if (cudaEventCreateWithFlags(&s->ev_kernel[i], cudaEventDisableTiming) != cudaSuccess ||
         cudaEventCreateWithFlags(&s->ev_copy[i], cudaEventDisableTiming) != cudaSuccess)
       return fail(infoli__fail(INFOLI_ERR_CUDA, "event creation failed"));
   if (cudaEventCreate(&s->ev_t0) != cudaSuccess || cudaEventCreate(&s->ev_t1) != cudaSuccess)
     return fail(infoli__fail(INFOLI_ERR_CUDA, "event creation failed"));
+  const Plan& pl = s->plan;
+  s->dev_bytes = (int64_t)(pl.cta.size() * sizeof(CtaWork) + pl.tiles.size() * sizeof(TileDesc) +
+                           pl.chunks.size() * sizeof(ChunkDesc) + pl.cell_slots.size() * sizeof(CellSlots) +
+                           pl.edges.size() * sizeof(uint16_t) + pl.edge_g.size() * sizeof(float) +
+                           pl.probes.size() * sizeof(int) + pl.gdesc.size() * sizeof(int2_t)) +
+                 (int64_t)np * (2 * sizeof(float) + F_COUNT * sizeof(float) + sizeof(double)) + 256 +
+                 (pl.shape.stamped ? (int64_t)np * 2 * sizeof(unsigned long long) : 0);
   *out = s;
+  return INFOLI_OK;
+}
+
+int infoli_sim_memory(infoli_sim* s, int64_t* device_bytes) {
+  infoli__clear_error();
+  if (!s || !device_bytes) return infoli__fail(INFOLI_ERR_ARG, "sim_memory: bad argument");
+  *device_bytes = s->dev_bytes;
   return INFOLI_OK;
 }
 
@@ -366,13 +424,14 @@ int infoli_sim_set_stimulus_cells(infoli_sim* s, const float* amp, const int* on
   if (!s || !amp || !onset || duration < 0) return infoli__fail(INFOLI_ERR_ARG, "set_stimulus_cells: bad argument");
   CK(cudaSetDevice(s->device));
   if (!s->d_cell_amp) {
-    CK(cudaMalloc((void**)&s->d_cell_amp, (size_t)s->n_pad * sizeof(float)));
-    CK(cudaMalloc((void**)&s->d_cell_onset, (size_t)s->n_pad * sizeof(int)));
-    CK(cudaMemset(s->d_cell_amp, 0, (size_t)s->n_pad * sizeof(float)));
-    CK(cudaMemset(s->d_cell_onset, 0, (size_t)s->n_pad * sizeof(int)));
+    CK(pool_alloc(&s->d_cell_amp, (size_t)s->n_pad * sizeof(float), s->device, s->stream));
+    CK(pool_alloc(&s->d_cell_onset, (size_t)s->n_pad * sizeof(int), s->device, s->stream));
+    CK(cudaMemsetAsync(s->d_cell_amp, 0, (size_t)s->n_pad * sizeof(float), s->stream));
+    CK(cudaMemsetAsync(s->d_cell_onset, 0, (size_t)s->n_pad * sizeof(int), s->stream));
   }
-  CK(cudaMemcpy(s->d_cell_amp, amp, (size_t)s->n * sizeof(float), cudaMemcpyHostToDevice));
-  CK(cudaMemcpy(s->d_cell_onset, onset, (size_t)s->n * sizeof(int), cudaMemcpyHostToDevice));
+  CK(cudaMemcpyAsync(s->d_cell_amp, amp, (size_t)s->n * sizeof(float), cudaMemcpyHostToDevice, s->stream));
+  CK(cudaMemcpyAsync(s->d_cell_onset, onset, (size_t)s->n * sizeof(int), cudaMemcpyHostToDevice, s->stream));
+  CK(cudaStreamSynchronize(s->stream));
   s->stim_kind = STIM_CELL;
   s->stim_dur = duration;
   return INFOLI_OK;
@@ -396,14 +455,15 @@ int infoli_sim_run(infoli_sim* s, int n_steps, int trace_every, int trace_what, 
     const int rows_needed = count_rows(0, launch_steps + trace_every, trace_every) + 1;
     const size_t want = std::min(need, (size_t)rows_needed * row_floats);
     if (s->trace_slot_floats < want) {
+      CK(cudaStreamSynchronize(s->stream));
       for (int i = 0; i < 2; ++i) {
-        if (s->d_trace[i]) cudaFree(s->d_trace[i]);
+        if (s->d_trace[i]) cudaFreeAsync(s->d_trace[i], s->stream);
         if (s->h_trace[i]) cudaFreeHost(s->h_trace[i]);
         s->d_trace[i] = nullptr;
         s->h_trace[i] = nullptr;
       }
       for (int i = 0; i < 2; ++i) {
-        CK(cudaMalloc((void**)&s->d_trace[i], want * sizeof(float)));
+        CK(pool_alloc(&s->d_trace[i], want * sizeof(float), s->device, s->stream));
         CK(cudaMallocHost((void**)&s->h_trace[i], want * sizeof(float)));
       }
       s->trace_slot_floats = want;
@@ -485,6 +545,58 @@ int infoli_sim_run(infoli_sim* s, int n_steps, int trace_every, int trace_what, 
   if (rc) return rc;
   s->step += n_steps;
   return INFOLI_OK;
+}
+
+int infoli_sim_launch(infoli_sim* s, int n_steps) {
+  infoli__clear_error();
+  if (!s || n_steps < 0) return infoli__fail(INFOLI_ERR_ARG, "sim_launch: bad argument");
+  CK(cudaSetDevice(s->device));
+  StepArgs a;
+  fill_args(s, &a);
+  a.trace_every = 0;
+  a.trace_mask = 0;
+  a.trace_nq = 0;
+  a.trace = nullptr;
+  int done = 0;
+  while (done < n_steps) {
+    const int len = std::min(kMaxStepsPerLaunch, n_steps - done);
+    a.step0 = s->step + done;
+    a.n_steps = len;
+    CK(cudaMemsetAsync(s->d_bar, 0, sizeof(unsigned), s->stream));
+    if (s->plan.shape.stamped) {
+      CK(cudaMemsetAsync(s->d_vll[0], 0xff, (size_t)s->n_pad * sizeof(unsigned long long), s->stream));
+      CK(cudaMemsetAsync(s->d_vll[1], 0xff, (size_t)s->n_pad * sizeof(unsigned long long), s->stream));
+    }
+    CK(launch_step_kernel(a, s->plan.grid, s->plan.threads, s->stream));
+    done += len;
+  }
+  CK(cudaEventRecord(s->ev_t1, s->stream));
+  s->step += n_steps;
+  s->async_pending = 1;
+  return INFOLI_OK;
+}
+
+int infoli_sim_query(infoli_sim* s) {
+  infoli__clear_error();
+  if (!s) return infoli__fail(INFOLI_ERR_ARG, "null handle");
+  if (!s->async_pending) return 1;
+  CK(cudaSetDevice(s->device));
+  const cudaError_t e = cudaEventQuery(s->ev_t1);
+  if (e == cudaErrorNotReady) return 0;
+  CK(e);
+  s->async_pending = 0;
+  const int rc = check_device_error(s);
+  return rc ? rc : 1;
+}
+
+int infoli_sim_sync(infoli_sim* s) {
+  infoli__clear_error();
+  if (!s) return infoli__fail(INFOLI_ERR_ARG, "null handle");
+  CK(cudaSetDevice(s->device));
+  CK(cudaStreamSynchronize(s->stream));
+  if (!s->async_pending) return INFOLI_OK;
+  s->async_pending = 0;
+  return check_device_error(s);
 }
 
 namespace {
@@ -589,13 +701,14 @@ int infoli_sim_set_profiling(infoli_sim* s, int on) {
   CK(cudaSetDevice(s->device));
   CK(cudaStreamSynchronize(s->stream));
   if (!on) {
-    if (s->d_prof) cudaFree(s->d_prof);
+    if (s->d_prof) cudaFreeAsync(s->d_prof, s->stream);
     s->d_prof = nullptr;
     return INFOLI_OK;
   }
   const size_t bytes = (size_t)s->plan.grid * kProfSlots * sizeof(unsigned long long);
-  if (!s->d_prof) CK(cudaMalloc((void**)&s->d_prof, bytes));
-  CK(cudaMemset(s->d_prof, 0, bytes));
+  if (!s->d_prof) CK(pool_alloc(&s->d_prof, bytes, s->device, s->stream));
+  CK(cudaMemsetAsync(s->d_prof, 0, bytes, s->stream));
+  CK(cudaStreamSynchronize(s->stream));
   return INFOLI_OK;
 }
 

@@ -257,3 +257,41 @@ int infoli_gen_bitmask(int n, float p, uint64_t seed, uint32_t* bits) {
   }
   return INFOLI_OK;
 }
+
+/* CSR of infoli_gen_bitmask's matrix without building the bitmask: the same
+ * per-receiver streams, one pass to count each row and one to fill it, both
+ * parallel over receivers. */
+int infoli_gen_bitmask_csr(int n, float p, uint64_t seed, int64_t* row_ptr, int32_t* col, int64_t cap,
+                           int64_t* n_edges) {
+  infoli__clear_error();
+  if (n <= 0 || !row_ptr || !(p >= 0.0f) || cap < 0 || (cap > 0 && !col))
+    return infoli__fail(INFOLI_ERR_ARG, "gen_bitmask_csr: bad argument");
+  const double pt = (double)p * 16777216.0;
+  const uint32_t thr = pt >= 16777216.0 ? 16777216u : (uint32_t)pt;
+  row_ptr[0] = 0;
+#pragma omp parallel for schedule(dynamic, 16)
+  for (int r = 0; r < n; r++) {
+    uint64_t st = seed + (uint64_t)(r + 1) * 0x632BE59BD9B4E019ull;
+    int64_t k = 0;
+    for (int s = 0; s < n; s++) {
+      if (s == r) continue;
+      if ((uint32_t)(sm64_next(&st) >> 40) < thr) k++;
+    }
+    row_ptr[r + 1] = k;
+  }
+  for (int r = 0; r < n; r++) row_ptr[r + 1] += row_ptr[r];
+  const int64_t e = row_ptr[n];
+  if (n_edges) *n_edges = e;
+  if (e > cap) return infoli__fail(INFOLI_ERR_CAPACITY, "gen_bitmask_csr: %lld edges exceed capacity %lld",
+                                   (long long)e, (long long)cap);
+#pragma omp parallel for schedule(dynamic, 16)
+  for (int r = 0; r < n; r++) {
+    uint64_t st = seed + (uint64_t)(r + 1) * 0x632BE59BD9B4E019ull;
+    int64_t k = row_ptr[r];
+    for (int s = 0; s < n; s++) {
+      if (s == r) continue;
+      if ((uint32_t)(sm64_next(&st) >> 40) < thr) col[k++] = s;
+    }
+  }
+  return INFOLI_OK;
+}

@@ -284,8 +284,10 @@ __device__ __forceinline__ void couple_packed(const unsigned char* sm, const Sme
 }
 
 // Phase A for one staged tile: warp w reduces chunks cb+w, cb+w+nwarps, ...
-// Each lane takes edges lane, lane+32, ... of the chunk (predicated, fully
-// unrolled); a shuffle tree sums the lanes; lane 0 writes the chunk's slot.
+// Each lane takes edges lane, lane+32, ... of the chunk (in unrolled,
+// predicated blocks of kChunkEdges; chunks of dense rows are longer, so a
+// CTA's partial-sum slots fit in shared memory); a shuffle tree sums the
+// lanes; lane 0 writes the chunk's slot.
 template <bool KAHAN, bool EDGE_G>
 __device__ __forceinline__ void couple_tile(const ChunkDesc* chunks, const uint16_t* edges, const float* edge_g,
                                             int cb, int ce, int edge0, const float* buf, const float* sVd,
@@ -295,9 +297,10 @@ __device__ __forceinline__ void couple_tile(const ChunkDesc* chunks, const uint1
     const float vc = sVd[c.recv];
     const int eb = c.edge_begin - edge0;
     float acc = 0.0f, comp = 0.0f;
+    for (int u0 = 0; u0 < c.count; u0 += kChunkEdges) {
 #pragma unroll
     for (int q = 0; q < kChunkEdges / 32; ++q) {
-      const int u = lane + 32 * q;
+      const int u = u0 + lane + 32 * q;
       if (u < c.count) {
         const int e = eb + u;
         const float V = vc - buf[edges[e]];
@@ -316,6 +319,7 @@ __device__ __forceinline__ void couple_tile(const ChunkDesc* chunks, const uint1
           acc += term;
         }
       }
+    }
     }
     if (KAHAN) {
       // carry the compensation separately through the tree

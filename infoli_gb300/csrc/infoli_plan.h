@@ -10,8 +10,10 @@
 //     16-byte-aligned ranges of the V_dend array that are staged into shared
 //     memory by a bulk async copy each step;
 //   * the edges of a (receiver, tile) pair are cut into chunks of at most
-//     kChunkEdges; one warp reduces one chunk into one partial-sum slot; the
-//     update thread adds its receiver's slots in sender order.
+//     kChunkEdges edges (a multiple of it for dense networks, whose slots
+//     would not fit in shared memory otherwise); one warp reduces one chunk
+//     into one partial-sum slot; the update thread adds its receiver's slots
+//     in sender order.
 // Edge entries are 16-bit offsets from the tile start (a tile is at most
 // 65536 floats), so one gather from shared memory per edge.
 //
@@ -32,7 +34,7 @@
 namespace infoli {
 #endif
 
-enum { kChunkEdges = 128 };
+enum { kChunkEdges = 128, kMaxChunkEdges = 8192 };
 
 // Packed layout of stamped plans.  A lane-chunk is up to kLaneEdges edges of
 // one receiver reduced by ONE lane; 32 lane-chunks form a group handled by
@@ -69,7 +71,7 @@ typedef struct {
   int recv;         //   kernel loads {slot, recv} as one 8-byte word)
                     // receiver, relative to the CTA's cell_begin
   int edge_begin;   // absolute index into the edge-offset (and per-edge g) arrays
-  int count;        // edges in this chunk, 1..kChunkEdges
+  int count;        // edges in this chunk, 1 .. the plan's chunk length
 } ChunkDesc;
 
 #if defined(__CUDACC__)

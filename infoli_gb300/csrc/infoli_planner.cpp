@@ -331,6 +331,9 @@ bool make_plan(const PlanInput& in, Plan* out, std::string* err) {
 
   // ---- tile capacity: one buffer holding the whole window when it fits,
   // otherwise two buffers for overlapped staging; shrink until smem fits.
+  // chunk length: kChunkEdges, doubled while the partial-sum slots crowd out
+  // the tiles
+  int chunk = kChunkEdges;
   auto slots_for = [&](int b, const std::vector<TileSpan>& tl) {
     int s = 0;
     for (int c = starts[b]; c < starts[b + 1]; ++c) {
@@ -345,7 +348,7 @@ bool make_plan(const PlanInput& in, Plan* out, std::string* err) {
           ++cnt;
           ++k;
         }
-        s += (cnt + kChunkEdges - 1) / kChunkEdges;
+        s += (cnt + chunk - 1) / chunk;
       }
     }
     return s;
@@ -353,7 +356,7 @@ bool make_plan(const PlanInput& in, Plan* out, std::string* err) {
   int nbuf = 1, tile_cap = std::min(max_window, 65536);
   std::vector<std::vector<TileSpan>> tiles(ctas);
   int max_slots = 0;
-  for (int attempt = 0; attempt < 16; ++attempt) {
+  for (int attempt = 0; attempt < 32; ++attempt) {
     if (max_window > tile_cap) nbuf = 2;
     max_slots = 0;
     for (int b = 0; b < ctas; ++b) {
@@ -362,6 +365,12 @@ bool make_plan(const PlanInput& in, Plan* out, std::string* err) {
     }
     max_slots = std::max(max_slots, 1);
     if (plan_smem_bytes(tile_cap, nbuf, threads, cells_cap, max_slots, in.kahan) <= in.smem_budget) break;
+    // slots taking over half of the budget: longer chunks first
+    if (plan_smem_bytes(0, 0, threads, cells_cap, max_slots, in.kahan) * 2 > in.smem_budget &&
+        chunk < kMaxChunkEdges) {
+      chunk *= 2;
+      continue;
+    }
     // shrink: give the tiles what is left after the fixed part
     size_t fixed = plan_smem_bytes(0, 0, threads, cells_cap, max_slots, in.kahan);
     size_t avail = in.smem_budget > fixed ? in.smem_budget - fixed : 0;
@@ -418,12 +427,12 @@ bool make_plan(const PlanInput& in, Plan* out, std::string* err) {
       for (int j = 0; j < (int)tl.size(); ++j) {
         std::vector<std::pair<int, float>> in_tile;
         while (k < snd.size() && snd[k].first < tl[j].hi) in_tile.push_back(snd[k++]);
-        for (size_t o = 0; o < in_tile.size(); o += kChunkEdges) {
+        for (size_t o = 0; o < in_tile.size(); o += chunk) {
           PendingChunk pc;
           pc.tile = j;
           pc.recv = r;
           pc.slot = slot++;
-          pc.e.assign(in_tile.begin() + o, in_tile.begin() + std::min(in_tile.size(), o + kChunkEdges));
+          pc.e.assign(in_tile.begin() + o, in_tile.begin() + std::min(in_tile.size(), o + (size_t)chunk));
           pend.push_back(std::move(pc));
         }
       }

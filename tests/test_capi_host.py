@@ -143,3 +143,16 @@ def test_sim_create_rejects_bad_arguments_without_crashing(capi):
         capi.Simulation(2, conf, rp, col, init_values=conf[23:])
     # on a machine without a GPU the device check fails first
     assert e.value.code in (capi.ERR_ARG, capi.ERR_CUDA)
+
+
+def test_bitmask_generator_csr_form_matches(built):
+    from infoli_gb300 import capi
+
+    for n, p, seed in [(100, 0.1, 3), (777, 0.3, 5), (33, 1.0, 1), (64, 0.0, 2)]:
+        bits = capi.gen_bitmask(n, p, seed)
+        rp, col = capi.bitmask_to_csr(n, bits)
+        rp2, col2 = capi.gen_bitmask_csr(n, p, seed)
+        assert np.array_equal(rp, rp2) and np.array_equal(col, col2)
+        assert not any(r in col[rp[r]:rp[r + 1]] for r in range(n))  # no self edges
+        if n > 100:
+            assert abs(len(col) / (n * (n - 1)) - p) < 0.01
