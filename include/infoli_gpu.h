@@ -144,6 +144,41 @@ int infoli_gen_bitmask(int n, float p, uint64_t seed, uint32_t* bits);
 int infoli_gen_bitmask_csr(int n, float p, uint64_t seed, int64_t* row_ptr, int32_t* col, int64_t cap,
                            int64_t* n_edges);
 
+/* Connectivity files of the reference's older simulator
+ * (src/truncated/openmp-oldAPI/infoli.c:262-350), read into CSR by receiver
+ * with per-edge conductances (same output contract as infoli_gen_uniform,
+ * plus g[cap]); conductances below 1e-7 are no connection.
+ *   dense:   n lines of n values, value j of line i = conductance from
+ *            sender i to receiver j (writers: tools/connectivity/percentage,
+ *            3d_gaussian, 3d_synapse_count); receivers list senders ascending;
+ *   triples: lines "send rec g" (tools/connectivity/3d_gaussian_compressed,
+ *            3d_synapse_count); receivers list senders in file order.
+ * A short dense file, a malformed line or an id outside [0, n) is
+ * INFOLI_ERR_CONFIG (the reference reads past such input silently). */
+int infoli_read_conn_dense(const char* path, int n, int64_t* row_ptr, int32_t* col, float* g, int64_t cap,
+                           int64_t* n_edges);
+int infoli_read_conn_triples(const char* path, int n, int64_t* row_ptr, int32_t* col, float* g, int64_t cap,
+                             int64_t* n_edges);
+
+/* Per-step stimulus file (-i; src/utils/utils.c:70-122 ReadFileLine): one
+ * line per step, the first n space-separated values of a line are the cells'
+ * iApp for that step.  Fills table[rows][n] (capacity max_rows rows; table
+ * may be NULL with max_rows 0 to count lines) and sets *rows.
+ * INFOLI_ERR_CAPACITY when the file has more lines than max_rows (*rows is
+ * still the line count); a line with fewer than n values is
+ * INFOLI_ERR_CONFIG with the reference's message. */
+int infoli_read_stim_file(const char* path, int n, float* table, int64_t max_rows, int64_t* rows);
+
+/* Randomised initial state (the reference's RAND_INIT, intended behaviour in
+ * src/single_threaded/infoli.c:206-236, a placeholder in
+ * src/openmp/infoli.c:402-422): srand(seed), then g_CaL[c] = 0.6 +
+ * 0.2 * (rand() % 100) / 100 for every cell, then every cell c runs
+ * k = (rand() % ceil(100 / DELTA)) | 1 steps on its own (no coupling current,
+ * no stimulus) from its state in state[19 * n], which is overwritten with the
+ * result.  Uses the C library's rand() like the reference (process-wide
+ * generator state).  The isolated steps run on the GPU. */
+int infoli_random_init(const float* params, int n, unsigned seed, float* state, int device);
+
 /* ------------------------------------------------------------------------ */
 /* one simulation on the GPU                                                */
 /* ------------------------------------------------------------------------ */
@@ -182,6 +217,11 @@ int infoli_sim_create(const infoli_sim_desc* desc, infoli_sim** out);
 int infoli_sim_set_stimulus_pulse(infoli_sim* s, int start_step, int end_step, float amp);
 /* Per-cell pulses: amp[c] for onset[c] <= step < onset[c] + duration. */
 int infoli_sim_set_stimulus_cells(infoli_sim* s, const float* amp, const int* onset, int duration);
+/* Per-step stimulus table (the reference's stimulus file): table[r][c] is
+ * cell c's iApp at step first_step + r, for rows rows; the table is copied
+ * to the device.  Runs must stay inside [first_step, first_step + rows)
+ * (INFOLI_ERR_ARG otherwise). */
+int infoli_sim_set_stimulus_table(infoli_sim* s, const float* table, int rows, int first_step);
 
 /* Replaces the time-step loop (src/openmp/infoli.c:478-698): advances
  * n_steps explicit-Euler steps.  When trace_every > 0, the selected

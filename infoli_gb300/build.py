@@ -23,7 +23,8 @@ OUT = os.path.join(HERE, "_build")
 INC = os.path.join(os.path.dirname(HERE), "include")
 
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
-CU_SOURCES = ["infoli_kernels.cu", "infoli_capi.cu", "infoli_static.cu", "infoli_batch.cu", "infoli_serve.cu"]
+CU_SOURCES = ["infoli_kernels.cu", "infoli_capi.cu", "infoli_static.cu", "infoli_batch.cu", "infoli_serve.cu",
+              "infoli_init.cu"]
 CXX_SOURCES = ["infoli_planner.cpp"]
 C_SOURCES = ["infoli_host.c", "infoli_trace.c"]
 

@@ -42,7 +42,9 @@ EXPORTED = [
     "infoli_sim_last_run_stats", "infoli_sim_plan_info", "infoli_sim_destroy", "infoli_format_f8",
     "infoli_format_row", "infoli_sim_set_profiling", "infoli_sim_get_profile", "infoli_plan_emulate",
     "infoli_run_noalloc", "infoli_sim_launch", "infoli_sim_query", "infoli_sim_sync",
-    "infoli_sim_memory", "infoli_gen_bitmask_csr", "infoli_gen_bitmask", "infoli_batch_create", "infoli_batch_set_stimulus_pulse",
+    "infoli_sim_memory", "infoli_gen_bitmask_csr",
+    "infoli_read_conn_dense", "infoli_read_conn_triples", "infoli_read_stim_file", "infoli_random_init",
+    "infoli_sim_set_stimulus_table", "infoli_gen_bitmask", "infoli_batch_create", "infoli_batch_set_stimulus_pulse",
     "infoli_batch_run", "infoli_batch_get_state", "infoli_batch_set_state", "infoli_batch_info",
     "infoli_batch_cta_info",
     "infoli_batch_destroy", "infoli_server_create", "infoli_server_submit", "infoli_server_poll",
@@ -178,6 +180,11 @@ def load():
         "infoli_sim_get_profile": ([P, P, P], I),
         "infoli_gen_bitmask": ([I, F, C.c_uint64, P], I),
         "infoli_gen_bitmask_csr": ([I, F, C.c_uint64, P, P, I64, P], I),
+        "infoli_read_conn_dense": ([C.c_char_p, I, P, P, P, I64, P], I),
+        "infoli_read_conn_triples": ([C.c_char_p, I, P, P, P, I64, P], I),
+        "infoli_read_stim_file": ([C.c_char_p, I, P, I64, P], I),
+        "infoli_random_init": ([P, I, U, P, I], I),
+        "infoli_sim_set_stimulus_table": ([P, P, I, I], I),
         "infoli_batch_create": ([C.POINTER(BatchDesc), C.POINTER(C.c_void_p)], I),
         "infoli_batch_set_stimulus_pulse": ([P, I, I, F], I),
         "infoli_batch_run": ([P, I], I),
@@ -272,6 +279,51 @@ def bitmask_to_csr(n: int, bits: np.ndarray):
         bits.view(np.uint8)).sum()) + 16)
 
 
+def _read_conn(fn, path, n):
+    row_ptr = np.zeros(n + 1, dtype=np.int64)
+    ne = C.c_int64(0)
+    cap = 0
+    while True:
+        col = np.zeros(max(cap, 1), dtype=np.int32)
+        g = np.zeros(max(cap, 1), dtype=np.float32)
+        rc = fn(os.fsencode(path), n, _p(row_ptr), _p(col), _p(g), cap, C.byref(ne))
+        if rc == ERR_CAPACITY and cap < ne.value:
+            cap = int(ne.value)
+            continue
+        _check(rc)
+        return row_ptr, col[: ne.value].copy(), g[: ne.value].copy()
+
+
+def read_conn_dense(path: str, n: int):
+    """(row_ptr, col, g) from an n x n conductance matrix file (row = sender)."""
+    return _read_conn(load().infoli_read_conn_dense, path, n)
+
+
+def read_conn_triples(path: str, n: int):
+    """(row_ptr, col, g) from a "send rec g" triples file."""
+    return _read_conn(load().infoli_read_conn_triples, path, n)
+
+
+def read_stim_file(path: str, n: int) -> np.ndarray:
+    """[rows, n] float32 per-step stimulus table."""
+    L = load()
+    rows = C.c_int64(0)
+    rc = L.infoli_read_stim_file(os.fsencode(path), n, None, 0, C.byref(rows))
+    if rc != ERR_CAPACITY:
+        _check(rc)
+    tab = np.zeros((rows.value, n), dtype=np.float32)
+    _check(L.infoli_read_stim_file(os.fsencode(path), n, _p(tab), rows.value, C.byref(rows)))
+    return tab
+
+
+def random_init(params, state: np.ndarray, seed: int, device: int = 0) -> np.ndarray:
+    """Randomised initial state (infoli_random_init); returns a new [19, n] array."""
+    st = np.ascontiguousarray(state, dtype=np.float32).copy()
+    prm = np.ascontiguousarray(params, dtype=np.float32)[:NPARAM].copy()
+    _check(load().infoli_random_init(_p(prm), st.shape[1], int(seed) & 0xFFFFFFFF, _p(st), int(device)))
+    return st
+
+
 def format_f8(v: float) -> str:
     buf = C.create_string_buffer(64)
     k = load().infoli_format_f8(buf, float(v))
@@ -363,6 +415,11 @@ class Simulation:
 
     def set_stimulus_pulse(self, start, end, amp):
         _check(self._L.infoli_sim_set_stimulus_pulse(self._h, int(start), int(end), float(amp)))
+
+    def set_stimulus_table(self, table, first_step=0):
+        self._tab = np.ascontiguousarray(table, dtype=np.float32)
+        assert self._tab.ndim == 2 and self._tab.shape[1] == self.n
+        _check(self._L.infoli_sim_set_stimulus_table(self._h, _p(self._tab), self._tab.shape[0], int(first_step)))
 
     def set_stimulus_cells(self, amp, onset, duration):
         self._amp = np.ascontiguousarray(amp, dtype=np.float32)

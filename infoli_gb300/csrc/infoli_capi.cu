@@ -114,6 +114,8 @@ struct infoli_sim {
   float* d_cell_amp = nullptr;
   int* d_cell_onset = nullptr;
   int stim_dur = 0;
+  float* d_stim_table = nullptr;  // STIM_TABLE: [stim_rows][n_pad]
+  int stim_rows = 0, stim_first = 0;
   // sync
   unsigned* d_bar = nullptr;
   int* d_err = nullptr;
@@ -140,7 +142,7 @@ void release(infoli_sim* s) {
   void* dptrs[] = {s->d_cta,   s->d_tiles,  s->d_chunks, s->d_cell_slots, s->d_edges,
                    s->d_edge_g, s->d_vd[0], s->d_vd[1],  s->d_st,         s->d_ca,
                    s->d_cell_amp, s->d_cell_onset, s->d_bar, s->d_err, s->d_trace[0], s->d_trace[1],
-                   s->d_prof, s->d_probes, s->d_vll[0], s->d_vll[1], s->d_gdesc};
+                   s->d_prof, s->d_probes, s->d_vll[0], s->d_vll[1], s->d_gdesc, s->d_stim_table};
   if (s->stream) {
     for (void* p : dptrs)
       if (p) cudaFreeAsync(p, s->stream);
@@ -437,12 +439,46 @@ int infoli_sim_set_stimulus_cells(infoli_sim* s, const float* amp, const int* on
   return INFOLI_OK;
 }
 
+int infoli_sim_set_stimulus_table(infoli_sim* s, const float* table, int rows, int first_step) {
+  infoli__clear_error();
+  if (!s || !table || rows <= 0) return infoli__fail(INFOLI_ERR_ARG, "set_stimulus_table: bad argument");
+  CK(cudaSetDevice(s->device));
+  CK(cudaStreamSynchronize(s->stream));
+  if (s->d_stim_table) cudaFreeAsync(s->d_stim_table, s->stream);
+  s->d_stim_table = nullptr;
+  const size_t np = (size_t)s->n_pad;
+  CK(pool_alloc(&s->d_stim_table, (size_t)rows * np * sizeof(float), s->device, s->stream));
+  CK(cudaMemsetAsync(s->d_stim_table, 0, (size_t)rows * np * sizeof(float), s->stream));
+  CK(cudaMemcpy2DAsync(s->d_stim_table, np * sizeof(float), table, (size_t)s->n * sizeof(float),
+                       (size_t)s->n * sizeof(float), (size_t)rows, cudaMemcpyHostToDevice, s->stream));
+  CK(cudaStreamSynchronize(s->stream));
+  s->stim_kind = STIM_TABLE;
+  s->stim_rows = rows;
+  s->stim_first = first_step;
+  return INFOLI_OK;
+}
+
+namespace {
+// A table stimulus covers [stim_first, stim_first + stim_rows); runs stay inside.
+int check_table_range(const infoli_sim* s, int n_steps) {
+  if (s->stim_kind != STIM_TABLE) return INFOLI_OK;
+  if (s->step < s->stim_first || (long long)s->step + n_steps > (long long)s->stim_first + s->stim_rows)
+    return infoli__fail(INFOLI_ERR_ARG, "run of steps %d..%lld leaves the stimulus table (steps %d..%lld)", s->step,
+                        (long long)s->step + n_steps - 1, s->stim_first, (long long)s->stim_first + s->stim_rows - 1);
+  return INFOLI_OK;
+}
+const float* table_at(const infoli_sim* s, int step0) {
+  return s->stim_kind == STIM_TABLE ? s->d_stim_table + (size_t)(step0 - s->stim_first) * s->n_pad : nullptr;
+}
+}  // namespace
+
 int infoli_sim_run(infoli_sim* s, int n_steps, int trace_every, int trace_what, infoli_trace_cb cb, void* user) {
   infoli__clear_error();
   if (!s || n_steps < 0) return infoli__fail(INFOLI_ERR_ARG, "sim_run: bad argument");
   if (trace_every > 0 && (!cb || nq_of(trace_what) == 0))
     return infoli__fail(INFOLI_ERR_ARG, "sim_run: tracing needs a callback and at least one quantity");
   CK(cudaSetDevice(s->device));
+  if (int rc0 = check_table_range(s, n_steps)) return rc0;
   const int nq = trace_every > 0 ? nq_of(trace_what) : 0;
   const size_t row_floats = (size_t)nq * s->n_pad;
 
@@ -504,6 +540,7 @@ int infoli_sim_run(infoli_sim* s, int n_steps, int trace_every, int trace_what, 
     const int slot = li & 1;
     a.step0 = s->step + done;
     a.n_steps = len;
+    a.stim_table = table_at(s, a.step0);
     a.trace = nq ? s->d_trace[slot] : nullptr;
     const int rows = count_rows(a.step0, len, trace_every);
     // the slot's previous contents must have been copied and consumed
@@ -551,6 +588,7 @@ int infoli_sim_launch(infoli_sim* s, int n_steps) {
   infoli__clear_error();
   if (!s || n_steps < 0) return infoli__fail(INFOLI_ERR_ARG, "sim_launch: bad argument");
   CK(cudaSetDevice(s->device));
+  if (int rc0 = check_table_range(s, n_steps)) return rc0;
   StepArgs a;
   fill_args(s, &a);
   a.trace_every = 0;
@@ -562,6 +600,7 @@ int infoli_sim_launch(infoli_sim* s, int n_steps) {
     const int len = std::min(kMaxStepsPerLaunch, n_steps - done);
     a.step0 = s->step + done;
     a.n_steps = len;
+    a.stim_table = table_at(s, a.step0);
     CK(cudaMemsetAsync(s->d_bar, 0, sizeof(unsigned), s->stream));
     if (s->plan.shape.stamped) {
       CK(cudaMemsetAsync(s->d_vll[0], 0xff, (size_t)s->n_pad * sizeof(unsigned long long), s->stream));

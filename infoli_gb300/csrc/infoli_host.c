@@ -295,3 +295,148 @@ int infoli_gen_bitmask_csr(int n, float p, uint64_t seed, int64_t* row_ptr, int3
   }
   return INFOLI_OK;
 }
+
+/* ---- connectivity and stimulus files ------------------------------------ */
+
+#define INFOLI_MIN_COND 0.0000001f /* conductances below this are no connection */
+
+/* src/truncated/openmp-oldAPI/infoli.c:262-311: n lines of n conductances;
+ * value j of line i is the conductance from sender i to receiver j.  Two
+ * passes like the reference (count, then fill), so receivers list their
+ * senders in ascending order.  A short file is an error here (the reference
+ * would reuse the last value read). */
+int infoli_read_conn_dense(const char* path, int n, int64_t* row_ptr, int32_t* col, float* g, int64_t cap,
+                           int64_t* n_edges) {
+  infoli__clear_error();
+  if (!path || n <= 0 || !row_ptr || cap < 0 || (cap > 0 && (!col || !g)))
+    return infoli__fail(INFOLI_ERR_ARG, "read_conn_dense: bad argument");
+  FILE* f = fopen(path, "r");
+  if (!f) return infoli__fail(INFOLI_ERR_FILE, "Error: Couldn't open %s", path);
+  int64_t* cnt = (int64_t*)calloc((size_t)n + 1, sizeof(int64_t));
+  if (!cnt) {
+    fclose(f);
+    return infoli__fail(INFOLI_ERR_NOMEM, "read_conn_dense: out of memory");
+  }
+  float v;
+  for (int s = 0; s < n; s++)
+    for (int r = 0; r < n; r++) {
+      if (fscanf(f, "%f ", &v) != 1) {
+        free(cnt);
+        fclose(f);
+        return infoli__fail(INFOLI_ERR_CONFIG, "Error: %s holds fewer than %d x %d conductances (line %d)", path,
+                            n, n, s + 1);
+      }
+      if (!(v < INFOLI_MIN_COND)) cnt[r + 1]++;
+    }
+  row_ptr[0] = 0;
+  for (int r = 0; r < n; r++) row_ptr[r + 1] = row_ptr[r] + cnt[r + 1];
+  const int64_t e = row_ptr[n];
+  if (n_edges) *n_edges = e;
+  if (e > cap) {
+    free(cnt);
+    fclose(f);
+    return infoli__fail(INFOLI_ERR_CAPACITY, "read_conn_dense: %lld edges exceed capacity %lld", (long long)e,
+                        (long long)cap);
+  }
+  for (int r = 0; r < n; r++) cnt[r] = row_ptr[r];
+  rewind(f);
+  for (int s = 0; s < n; s++)
+    for (int r = 0; r < n; r++) {
+      if (fscanf(f, "%f ", &v) != 1) break; /* cannot happen: the first pass read them */
+      if (!(v < INFOLI_MIN_COND)) {
+        col[cnt[r]] = s;
+        g[cnt[r]] = v;
+        cnt[r]++;
+      }
+    }
+  free(cnt);
+  fclose(f);
+  return INFOLI_OK;
+}
+
+/* src/truncated/openmp-oldAPI/infoli.c:312-350: lines "send rec g"; receivers
+ * keep their senders in file order.  Ids outside [0, n) are an error (the
+ * reference would index out of bounds). */
+int infoli_read_conn_triples(const char* path, int n, int64_t* row_ptr, int32_t* col, float* g, int64_t cap,
+                             int64_t* n_edges) {
+  infoli__clear_error();
+  if (!path || n <= 0 || !row_ptr || cap < 0 || (cap > 0 && (!col || !g)))
+    return infoli__fail(INFOLI_ERR_ARG, "read_conn_triples: bad argument");
+  FILE* f = fopen(path, "r");
+  if (!f) return infoli__fail(INFOLI_ERR_FILE, "Error: Couldn't open %s", path);
+  int64_t* cnt = (int64_t*)calloc((size_t)n + 1, sizeof(int64_t));
+  if (!cnt) {
+    fclose(f);
+    return infoli__fail(INFOLI_ERR_NOMEM, "read_conn_triples: out of memory");
+  }
+  int snd, rec, rc;
+  float v;
+  long long line = 0;
+  while ((rc = fscanf(f, "%d %d %f\n", &snd, &rec, &v)) != EOF) {
+    line++;
+    if (rc != 3 || snd < 0 || snd >= n || rec < 0 || rec >= n) {
+      free(cnt);
+      fclose(f);
+      return infoli__fail(INFOLI_ERR_CONFIG, "Error: %s line %lld is not \"send rec g\" with ids below %d", path,
+                          line, n);
+    }
+    if (!(v < INFOLI_MIN_COND)) cnt[rec + 1]++;
+  }
+  row_ptr[0] = 0;
+  for (int r = 0; r < n; r++) row_ptr[r + 1] = row_ptr[r] + cnt[r + 1];
+  const int64_t e = row_ptr[n];
+  if (n_edges) *n_edges = e;
+  if (e > cap) {
+    free(cnt);
+    fclose(f);
+    return infoli__fail(INFOLI_ERR_CAPACITY, "read_conn_triples: %lld edges exceed capacity %lld", (long long)e,
+                        (long long)cap);
+  }
+  for (int r = 0; r < n; r++) cnt[r] = row_ptr[r];
+  rewind(f);
+  while (fscanf(f, "%d %d %f\n", &snd, &rec, &v) == 3) {
+    if (!(v < INFOLI_MIN_COND)) {
+      col[cnt[rec]] = snd;
+      g[cnt[rec]] = v;
+      cnt[rec]++;
+    }
+  }
+  free(cnt);
+  fclose(f);
+  return INFOLI_OK;
+}
+
+/* src/utils/utils.c:70-122 (ReadFileLine): one line per step, values
+ * separated by single spaces; the first n of a line are the cells' iApp
+ * (atof, stored as float).  A line with fewer than n space-separated fields
+ * is an error, counted like the reference (a trailing space before the
+ * newline counts as a field).  Lines have no length limit here. */
+int infoli_read_stim_file(const char* path, int n, float* table, int64_t max_rows, int64_t* rows) {
+  infoli__clear_error();
+  if (!path || n <= 0 || max_rows < 0 || (max_rows > 0 && !table) || !rows)
+    return infoli__fail(INFOLI_ERR_ARG, "read_stim_file: bad argument");
+  FILE* f = fopen(path, "r");
+  if (!f) return infoli__fail(INFOLI_ERR_FILE, "Error: Couldn't open %s", path);
+  char* line = NULL;
+  size_t len = 0;
+  int64_t r = 0;
+  while (getline(&line, &len, f) != -1) {
+    int i = 0;
+    char* save = NULL;
+    for (char* tok = strtok_r(line, " ", &save); tok; tok = strtok_r(NULL, " ", &save), i++)
+      if (i < n && r < max_rows) table[(size_t)r * n + i] = (float)atof(tok);
+    if (i < n) {
+      free(line);
+      fclose(f);
+      return infoli__fail(INFOLI_ERR_CONFIG, "Error: Input line doesn't have enough elements, only %d", i);
+    }
+    r++;
+  }
+  free(line);
+  fclose(f);
+  *rows = r;
+  if (r > max_rows)
+    return infoli__fail(INFOLI_ERR_CAPACITY, "read_stim_file: %lld lines exceed capacity %lld", (long long)r,
+                        (long long)max_rows);
+  return INFOLI_OK;
+}

@@ -19,8 +19,15 @@
  *     step printed untagged, no header (:194-197, :294-296).
  * Extensions: -s <seed> fixes the generator seed (default time(NULL));
  * -K enables Kahan-compensated coupling sums.  -i is accepted like the
- * reference (which ignores the stimulus file, :430-477); a per-step stimulus
- * file is read when -I <file> is given instead.
+ * reference (which opens and then ignores the stimulus file, :169-176,
+ * :430-477); -I <file> applies a per-step stimulus file in the reference's
+ * format (src/utils/utils.c:70-122), one line per step, and the run lasts as
+ * many steps as the file has lines (the intent of the disabled loop); the
+ * Input(Iapp) column then shows cell 0's value.  -m <file> / -M <file> read
+ * the connectivity from a dense conductance matrix / "send rec g" triples
+ * (src/truncated/openmp-oldAPI/infoli.c:262-350) instead of the generator.
+ * -R randomises the initial state (RAND_INIT, src/single_threaded/infoli.c:
+ * 206-236) with the -s seed.
  * Errors are reported like the reference (printf + exit(EXIT_FAILURE)).
  */
 #define _GNU_SOURCE
@@ -48,6 +55,9 @@ static void print_usage(void) {
   printf("-o denotes a filename for simulation output. Default value: InferiorOlive_Output.txt.\n");
   printf("-s denotes the connectivity generator seed. Default value: time(NULL).\n");
   printf("-K enables compensated (Kahan) coupling sums.\n");
+  printf("-I denotes a per-step stimulus file (one line of n values per step).\n");
+  printf("-m / -M denote a connectivity file: dense conductance matrix / send rec g triples.\n");
+  printf("-R randomises the initial state (seeded by -s).\n");
 }
 
 struct trace_ctx {
@@ -57,13 +67,16 @@ struct trace_ctx {
   int tagged;
   int stim_start, stim_end;
   float stim_amp;
+  const float* table; /* per-step stimulus (-I), row r = step r, or NULL */
+  int n;
 };
 
 static void on_trace(void* user, int step, int what, const float* v, int n) {
   struct trace_ctx* t = (struct trace_ctx*)user;
   (void)what;
   if (t->tagged) {
-    const float iApp = (step >= t->stim_start && step < t->stim_end) ? t->stim_amp : 0.0f;
+    const float iApp = t->table ? t->table[(size_t)step * t->n]
+                                : (step >= t->stim_start && step < t->stim_end) ? t->stim_amp : 0.0f;
     fprintf(t->out, " %d %.2f ", step + 1, iApp);
   }
   long long len = infoli_format_row(t->buf, t->cap, v, n, t->tagged, 0);
@@ -83,6 +96,9 @@ int main(int argc, char** argv) {
   char* paramsFileName = (char*)malloc(PATH_MAX);
   char* outFileName = (char*)"InferiorOlive_Output.txt";
   char* inFileName = NULL;
+  char* stimFileName = NULL;
+  char* connFileName = NULL;
+  int connTriples = 0, randInit = 0;
   char tempbuf[128];
 
   /* default.conf beside the executable (:113-121) */
@@ -98,7 +114,7 @@ int main(int argc, char** argv) {
   strcat(paramsFileName, "default.conf");
 
   int option;
-  while ((option = getopt(argc, argv, "hn:p:t:i:c:o:s:K")) != -1) {
+  while ((option = getopt(argc, argv, "hn:p:t:i:c:o:s:KI:m:M:R")) != -1) {
     switch (option) {
       case 'h':
         print_usage();
@@ -144,6 +160,17 @@ int main(int argc, char** argv) {
       case 'K':
         kahan = 1;
         break;
+      case 'I':
+        stimFileName = optarg;
+        break;
+      case 'm':
+      case 'M':
+        connFileName = optarg;
+        connTriples = option == 'M';
+        break;
+      case 'R':
+        randInit = 1;
+        break;
       default:
         print_usage();
         exit(EXIT_FAILURE);
@@ -186,21 +213,55 @@ int main(int argc, char** argv) {
   }
 #endif
 
-  /* connectivity (:306-375) */
+  /* connectivity (:306-375), or a connectivity file */
   int64_t* row_ptr = (int64_t*)malloc(sizeof(int64_t) * ((size_t)n + 1));
-  int64_t cap = (int64_t)((double)n * (n - 1) * (p * 1.05 + 0.001)) + 1024, ne = 0;
-  if (cap > (int64_t)n * (n - 1)) cap = (int64_t)n * (n - 1);
-  int32_t* col = (int32_t*)malloc(sizeof(int32_t) * (size_t)(cap > 0 ? cap : 1));
-  int rc = infoli_gen_uniform(n, p, seed, row_ptr, col, cap, &ne);
-  if (rc == INFOLI_ERR_CAPACITY) {
-    free(col);
-    cap = ne;
+  int64_t cap = 0, ne = 0;
+  int32_t* col = NULL;
+  float* gedge = NULL;
+  int rc;
+  if (connFileName) {
+    rc = connTriples ? infoli_read_conn_triples(connFileName, n, row_ptr, NULL, NULL, 0, &ne)
+                     : infoli_read_conn_dense(connFileName, n, row_ptr, NULL, NULL, 0, &ne);
+    if (rc == INFOLI_ERR_CAPACITY) {
+      cap = ne;
+      col = (int32_t*)malloc(sizeof(int32_t) * (size_t)(cap > 0 ? cap : 1));
+      gedge = (float*)malloc(sizeof(float) * (size_t)(cap > 0 ? cap : 1));
+      rc = connTriples ? infoli_read_conn_triples(connFileName, n, row_ptr, col, gedge, cap, &ne)
+                       : infoli_read_conn_dense(connFileName, n, row_ptr, col, gedge, cap, &ne);
+    }
+  } else {
+    cap = (int64_t)((double)n * (n - 1) * (p * 1.05 + 0.001)) + 1024;
+    if (cap > (int64_t)n * (n - 1)) cap = (int64_t)n * (n - 1);
     col = (int32_t*)malloc(sizeof(int32_t) * (size_t)(cap > 0 ? cap : 1));
     rc = infoli_gen_uniform(n, p, seed, row_ptr, col, cap, &ne);
+    if (rc == INFOLI_ERR_CAPACITY) {
+      free(col);
+      cap = ne;
+      col = (int32_t*)malloc(sizeof(int32_t) * (size_t)(cap > 0 ? cap : 1));
+      rc = infoli_gen_uniform(n, p, seed, row_ptr, col, cap, &ne);
+    }
   }
   if (rc != INFOLI_OK) {
+    printf("%s\n", infoli_last_error());
+    exit(EXIT_FAILURE);
+  }
+  if (randInit && infoli_random_init(conf, n, seed, state, 0) != INFOLI_OK) {
     printf("Error: %s\n", infoli_last_error());
     exit(EXIT_FAILURE);
+  }
+  /* per-step stimulus file */
+  float* stimTable = NULL;
+  int64_t stimRows = 0;
+  if (stimFileName) {
+    rc = infoli_read_stim_file(stimFileName, n, NULL, 0, &stimRows);
+    if (rc == INFOLI_OK || rc == INFOLI_ERR_CAPACITY) {
+      stimTable = (float*)malloc(sizeof(float) * (size_t)(stimRows > 0 ? stimRows : 1) * (size_t)n);
+      rc = infoli_read_stim_file(stimFileName, n, stimTable, stimRows, &stimRows);
+    }
+    if (rc != INFOLI_OK) {
+      printf("%s\n", infoli_last_error());
+      exit(EXIT_FAILURE);
+    }
   }
 
 #ifndef G_CAL_FROM_FILE
@@ -218,7 +279,7 @@ int main(int argc, char** argv) {
   d.init_state = state;
   d.row_ptr = row_ptr;
   d.col = col;
-  d.g = NULL;
+  d.g = gedge;
   d.g_uniform = conf[INFOLI_P_CONDUCTANCE];
   d.flags = kahan ? INFOLI_F_KAHAN : 0;
   d.device = 0;
@@ -228,6 +289,11 @@ int main(int argc, char** argv) {
     exit(EXIT_FAILURE);
   }
   free(col);
+  free(gedge);
+  if (stimTable && stimRows > 0 && infoli_sim_set_stimulus_table(sim, stimTable, (int)stimRows, 0) != INFOLI_OK) {
+    printf("Error: %s\n", infoli_last_error());
+    exit(EXIT_FAILURE);
+  }
 
   struct trace_ctx tc;
   tc.out = pOutFile;
@@ -241,8 +307,10 @@ int main(int argc, char** argv) {
   tc.stim_start = 20000;
   tc.stim_end = 20500 - 1;
   tc.stim_amp = 6.0f;
+  tc.table = stimTable;
+  tc.n = n;
 
-  const int total_simulation_steps = (int)(simTime / conf[INFOLI_P_DELTA]);
+  const int total_simulation_steps = stimTable ? (int)stimRows : (int)(simTime / conf[INFOLI_P_DELTA]);
   struct timeval tic, toc;
   gettimeofday(&tic, NULL);
   rc = infoli_sim_run(sim, total_simulation_steps, print_granularity, INFOLI_TRACE_AXON, on_trace, &tc);
@@ -269,5 +337,6 @@ int main(int argc, char** argv) {
   free(state);
   free(row_ptr);
   free(tc.buf);
+  free(stimTable);
   return 0;
 }

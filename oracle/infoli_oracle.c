@@ -49,18 +49,27 @@ enum {
 
 /* Stimulus kinds: 0 = one global pulse (the reference's hard-coded schedule,
  * src/openmp/infoli.c:482-485: amplitude a for start <= step < end);
- * 1 = per-cell pulse (amp[c] for onset[c] <= step < onset[c] + dur). */
+ * 1 = per-cell pulse (amp[c] for onset[c] <= step < onset[c] + dur);
+ * 2 = per-step table, one row of n values per step from `first` on (the
+ * reference's stimulus file, src/utils/utils.c:70-122, applied as in its
+ * disabled loop src/openmp/infoli.c:434-477: iAppIn = iAppArray[cell]); 0
+ * outside the table. */
 typedef struct {
     int kind;
     int start, end;       /* kind 0 */
     float amp;            /* kind 0 */
-    const float *cell_amp;  /* kind 1, [n] */
+    const float *cell_amp;  /* kind 1, [n]; kind 2, [rows][n] */
     const int *cell_onset;  /* kind 1, [n] */
-    int dur;                /* kind 1 */
+    int dur;                /* kind 1; kind 2: rows */
+    int n;                  /* kind 2 */
 } orc_stim;
 
 static inline float stim_f32(const orc_stim *s, int c, int step) {
     if (s->kind == 0) return (step >= s->start && step < s->end) ? s->amp : 0.0f;
+    if (s->kind == 2) {
+        const int r = step - s->start;
+        return (r >= 0 && r < s->dur) ? s->cell_amp[(size_t)r * s->n + c] : 0.0f;
+    }
     return (step >= s->cell_onset[c] && step < s->cell_onset[c] + s->dur) ? s->cell_amp[c] : 0.0f;
 }
 
@@ -251,6 +260,7 @@ static inline void cell_f32(const float *P, float **S, int c, float I_c, float i
  *   g         per-edge conductance, or NULL for g_uniform on every edge
  *   stim_kind 0: stim_i = {start, end}, stim_f = {amp}
  *             1: per-cell cell_amp[n], cell_onset[n], stim_i[0] = duration
+ *             2: table cell_amp[rows][n], stim_i = {first step, rows}
  *   trace_every  record after every step s with ((step0+s) % trace_every)==0
  *                (the reference's print rule, src/openmp/infoli.c:682); 0 = off
  *   tr_axon/tr_soma/tr_dend  [ntrace][n] each, any may be NULL
@@ -269,6 +279,7 @@ int orc_run_f32(int n, const float *params, float *state,
     memset(&st, 0, sizeof st);
     st.kind = stim_kind;
     if (stim_kind == 0) { st.start = stim_i[0]; st.end = stim_i[1]; st.amp = stim_f[0]; }
+    else if (stim_kind == 2) { st.cell_amp = cell_amp; st.start = stim_i[0]; st.dur = stim_i[1]; st.n = n; }
     else { st.cell_amp = cell_amp; st.cell_onset = cell_onset; st.dur = stim_i[0]; }
     if (nthreads < 1) nthreads = 1;
     int rows = 0;
@@ -419,6 +430,9 @@ int orc_run_f64(int n, const double *params, double *state,
         for (c = 0; c < n; c++) {
             double iapp;
             if (stim_kind == 0) iapp = (step >= stim_i[0] && step < stim_i[1]) ? (double)stim_f[0] : 0.0;
+            else if (stim_kind == 2)
+                iapp = (step - stim_i[0] >= 0 && step - stim_i[0] < stim_i[1])
+                           ? (double)cell_amp[(size_t)(step - stim_i[0]) * n + c] : 0.0;
             else iapp = (step >= cell_onset[c] && step < cell_onset[c] + stim_i[0]) ? (double)cell_amp[c] : 0.0;
             cell_f64(params, S, c, ic[c], iapp);
         }
@@ -432,6 +446,26 @@ int orc_run_f64(int n, const double *params, double *state,
     }
     free(ic);
     return rows;
+}
+
+/* Randomised initial state, the intent of RAND_INIT
+ * (src/single_threaded/infoli.c:206-236; placeholder in
+ * src/openmp/infoli.c:402-422): srand(seed); g_CaL[c] = 0.6 +
+ * 0.2 * (rand() % 100) / 100 for every cell, then for every cell
+ * k = (rand() % ceil(100 / DELTA)) | 1 steps of the cell alone (no coupling
+ * current, no stimulus).  state[19*n] is updated in place; steps_out[n] (may
+ * be NULL) receives k. */
+void orc_random_init(int n, const float *params, float *state, unsigned seed, int *steps_out) {
+    float *S[ORC_NSTATE];
+    for (int i = 0; i < ORC_NSTATE; i++) S[i] = state + (size_t)i * n;
+    srand(seed);
+    for (int c = 0; c < n; c++) S[S_G_CAL][c] = 0.6 + (0.2 * (rand() % 100) / 100);
+    const int span = (int)ceil(100 / params[P_DELTA]);
+    for (int c = 0; c < n; c++) {
+        const int k = (rand() % span) | 1;
+        if (steps_out) steps_out[c] = k;
+        for (int j = 0; j < k; j++) cell_f32(params, S, c, 0.0f, 0.0f);
+    }
 }
 
 int orc_max_threads(void) {

@@ -57,6 +57,8 @@ def lib():
         L.orc_run_f64.argtypes = a64
         L.orc_run_f64.restype = C.c_int
         L.orc_max_threads.restype = C.c_int
+        L.orc_random_init.argtypes = [C.c_int, P, P, C.c_uint, P]
+        L.orc_random_init.restype = None
         _lib = L
     return _lib
 
@@ -96,13 +98,19 @@ def default_state(n: int, init42: np.ndarray, dtype=np.float32) -> np.ndarray:
 
 
 def _stim_args(stim, n):
-    """stim = ('pulse', start, end, amp) or ('cell', amp[n], onset[n], dur)."""
+    """stim = ('pulse', start, end, amp), ('cell', amp[n], onset[n], dur) or
+    ('table', rows[k, n], first_step)."""
     if stim is None:
         stim = ("pulse", 20000, 20499, 6.0)
     if stim[0] == "pulse":
         si = np.array([stim[1], stim[2]], dtype=np.int32)
         sf = np.array([stim[3]], dtype=np.float32)
         return 0, si, sf, None, None
+    if stim[0] == "table":
+        tab = np.ascontiguousarray(stim[1], dtype=np.float32)
+        assert tab.ndim == 2 and tab.shape[1] == n
+        si = np.array([stim[2], tab.shape[0]], dtype=np.int32)
+        return 2, si, np.zeros(1, dtype=np.float32), tab, None
     amp = np.ascontiguousarray(stim[1], dtype=np.float32)
     onset = np.ascontiguousarray(stim[2], dtype=np.int32)
     assert amp.shape == (n,) and onset.shape == (n,)
@@ -138,6 +146,16 @@ def run(n, params, state, row_ptr, col, g=None, g_uniform=0.04, stim=None,
              _ptr(out["dend"]), int(nthreads))
     assert got == rows
     return {k: v[:rows] for k, v in out.items() if v is not None}
+
+
+def random_init(n, params, state, seed):
+    """Randomised initial state (orc_random_init); state (19, n) float32 is
+    updated in place; returns the isolated step count of every cell."""
+    assert state.dtype == np.float32 and state.shape == (19, n) and state.flags.c_contiguous
+    params = np.ascontiguousarray(params, dtype=np.float32)
+    steps = np.zeros(n, dtype=np.int32)
+    lib().orc_random_init(n, _ptr(params), _ptr(state), int(seed) & 0xFFFFFFFF, _ptr(steps))
+    return steps
 
 
 def max_threads() -> int:

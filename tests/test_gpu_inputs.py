@@ -1,0 +1,120 @@
+"""Inputs beyond the built-in generator, on the GPU path against the oracle:
+per-step stimulus tables (the reference's stimulus file), topologies read
+from connectivity files with per-edge conductances, randomised initial states
+(RAND_INIT), and the CLI options that use them."""
+import os
+import subprocess
+
+import numpy as np
+import pytest
+
+from helpers import CONF, TOL_VSOMA_MV, golden, hetero_state, kat_topology
+from oracle import oracle as O
+
+pytestmark = pytest.mark.gpu
+
+
+@pytest.fixture(scope="module")
+def ig(built):
+    import infoli_gb300
+
+    assert infoli_gb300.device_count() >= 1
+    return infoli_gb300
+
+
+@pytest.fixture(scope="module")
+def conf(built):
+    return O.read_parameters(CONF)
+
+
+def test_stimulus_table_vs_oracle(ig, conf):
+    n, steps = 300, 1200
+    rp, col = ig.gen_uniform(n, 0.2, 4)
+    rng = np.random.default_rng(5)
+    tab = np.zeros((steps, n), dtype=np.float32)
+    tab[100:600] = rng.uniform(0, 6, (1, n)).astype(np.float32)  # a step of current per cell
+    tab[700:] = rng.uniform(-1, 1, (steps - 700, n)).astype(np.float32)  # noise
+    st0 = hetero_state(conf, n, 6)
+    with ig.Simulation(n, conf, rp, col, init_state=st0) as sim:
+        sim.set_stimulus_table(tab)
+        gpu = sim.run(steps, 1, 2)["soma"]
+        with pytest.raises(ig.InfoliError):
+            sim.run(1)  # past the end of the table
+    ref = O.run(n, conf[:23], st0.copy(), rp, col, g_uniform=conf[1], stim=("table", tab, 0), nsteps=steps,
+                trace_every=1, traces=("soma",), nthreads=O.max_threads())["soma"]
+    assert np.max(np.abs(gpu[:600] - ref[:600])) <= TOL_VSOMA_MV
+    assert np.max(np.abs(gpu - ref)) <= 10 * TOL_VSOMA_MV
+
+
+def test_random_init_vs_oracle(ig, conf):
+    n = 2000
+    st = O.default_state(n, conf)
+    gpu = ig.random_init(conf, st, seed=11)
+    ref = st.copy()
+    k = O.random_init(n, conf[:23], ref, 11)
+    assert np.array_equal(gpu[O.S["g_CaL"]], ref[O.S["g_CaL"]])  # same draws, same float conversion
+    assert k.min() >= 1 and k.max() <= 1999 and np.all(k % 2 == 1)
+    for name in ("V_soma", "V_dend", "V_axon"):
+        assert np.max(np.abs(gpu[O.S[name]] - ref[O.S[name]])) <= TOL_VSOMA_MV, name
+    assert np.std(gpu[O.S["V_soma"]]) > 0.01  # the states really differ between cells
+
+
+def test_connectivity_files_through_the_gpu(ig, conf, tmp_path):
+    # triples with per-edge conductances in scrambled file order
+    rng = np.random.default_rng(8)
+    n = 500
+    rp, col, g = ig.gen_fixed_degree(n, 40, 9, g_range=(0.02, 0.06))
+    recv = np.repeat(np.arange(n), np.diff(rp))
+    order = rng.permutation(len(col))
+    f = tmp_path / "t.txt"
+    f.write_text("".join(f"{col[e]} {recv[e]} {g[e]:.6f}\n" for e in order))
+    rp2, col2, g2 = ig.read_conn_triples(str(f), n)
+    st0 = hetero_state(conf, n, 10)
+    # subthreshold pulse: the GPU sums each receiver's edges in ascending sender
+    # order, the reference in file order, and spikes would amplify that rounding
+    with ig.Simulation(n, conf, rp2, col2, g=g2, init_state=st0) as sim:
+        sim.set_stimulus_pulse(100, 300, 1.0)
+        gpu = sim.run(1000, 1, 2)["soma"]
+    ref = O.run(n, conf[:23], st0.copy(), rp2, col2, g=g2, stim=("pulse", 100, 300, 1.0), nsteps=1000,
+                trace_every=1, traces=("soma",), nthreads=O.max_threads())["soma"]
+    assert np.max(np.abs(gpu - ref)) <= TOL_VSOMA_MV
+
+
+def _cli(tmp_path, args):
+    from infoli_gb300 import build
+
+    exe = os.path.join(os.path.dirname(build.__file__), "_build", "infoli.x")
+    return subprocess.run([exe, *args], cwd=tmp_path, capture_output=True, text=True, timeout=300)
+
+
+def test_cli_file_inputs(ig, conf, tmp_path):
+    n, rp, col, g, _ = kat_topology()
+    G = golden("kat_stable_version.npz")["cond_sender_by_receiver"]
+    (tmp_path / "conn.txt").write_text("".join("".join(f"{v:f} " for v in row) + "\n" for row in G))
+    steps = 400
+    tab = np.zeros((steps, n), dtype=np.float32)
+    tab[50:250, ::2] = 5.0
+    (tmp_path / "stim.txt").write_text("".join(" ".join(f"{v:g}" for v in row) + "\n" for row in tab))
+    r = _cli(tmp_path, ["-n", str(n), "-m", "conn.txt", "-I", "stim.txt", "-o", "out.txt"])
+    assert r.returncode == 0, r.stdout + r.stderr
+    lines = open(tmp_path / "out.txt").read().split("\n")
+    # data rows: " %d %.2f " then the cells (the in-place rewrite of the first
+    # line leaves a line of spaces, as in the reference)
+    rows = [l for l in lines if l.startswith(" ") and l.strip()]
+    assert len(rows) == steps // 100  # trace every 100th step, run length = file lines
+    # last traced step (300) against the oracle on the same inputs
+    st = O.default_state(n, conf)
+    ref = O.run(n, conf[:23], st, rp, col, g=g, stim=("table", tab, 0), nsteps=301, trace_every=100,
+                traces=("axon",), nthreads=1)["axon"]
+    toks = rows[-1].split()
+    assert toks[0] == "301"
+    vals = np.array(toks[4::3], dtype=np.float64)
+    assert np.max(np.abs(vals - ref[-1])) <= 10 * TOL_VSOMA_MV
+    # randomised initial state: runs, and differs from the plain start
+    r = _cli(tmp_path, ["-n", "64", "-p", "0.2", "-t", "10", "-s", "3", "-R", "-o", "rand.txt"])
+    assert r.returncode == 0, r.stdout + r.stderr
+    r2 = _cli(tmp_path, ["-n", "64", "-p", "0.2", "-t", "10", "-s", "3", "-o", "plain.txt"])
+    assert r2.returncode == 0
+    first = [[l for l in open(tmp_path / f).read().split("\n") if l.startswith(" ") and l.strip()][0]
+             for f in ("rand.txt", "plain.txt")]
+    assert first[0] != first[1]
