@@ -102,6 +102,7 @@ struct infoli_sim {
   float* d_edge_g = nullptr;
   int* d_probes = nullptr;
   int2_t* d_gdesc = nullptr;
+  int32_t* d_gcol = nullptr;  // gather plans
   unsigned long long* d_vll[2] = {nullptr, nullptr};  // stamped exchange words
   // state
   float* d_vd[2] = {nullptr, nullptr};
@@ -142,7 +143,8 @@ void release(infoli_sim* s) {
   void* dptrs[] = {s->d_cta,   s->d_tiles,  s->d_chunks, s->d_cell_slots, s->d_edges,
                    s->d_edge_g, s->d_vd[0], s->d_vd[1],  s->d_st,         s->d_ca,
                    s->d_cell_amp, s->d_cell_onset, s->d_bar, s->d_err, s->d_trace[0], s->d_trace[1],
-                   s->d_prof, s->d_probes, s->d_vll[0], s->d_vll[1], s->d_gdesc, s->d_stim_table};
+                   s->d_prof, s->d_probes, s->d_vll[0], s->d_vll[1], s->d_gdesc, s->d_stim_table,
+                   s->d_gcol};
   if (s->stream) {
     for (void* p : dptrs)
       if (p) cudaFreeAsync(p, s->stream);
@@ -221,6 +223,7 @@ int fill_args(infoli_sim* s, StepArgs* a) {
   a->vll[1] = s->d_vll[1];
   a->probes = s->d_probes;
   a->gdesc = reinterpret_cast<const int2*>(s->d_gdesc);
+  a->gcol = s->d_gcol;
   a->n_cells = s->n;
   return INFOLI_OK;
 }
@@ -315,7 +318,11 @@ int infoli_sim_create(const infoli_sim_desc* d, infoli_sim** out) {
   pin.smem_budget = (size_t)smem_optin - 1024;  // static shared (abort flag) headroom
   pin.kahan = s->kahan;
   pin.no_resident = getenv("INFOLI_NO_RESIDENT") ? 1 : 0;
-  if (const char* sm = getenv("INFOLI_SYNC")) pin.sync_mode = !strcmp(sm, "barrier") ? kSyncBarrier : !strcmp(sm, "stamped") ? kSyncStamped : kSyncAuto;
+  if (const char* sm = getenv("INFOLI_SYNC"))
+    pin.sync_mode = !strcmp(sm, "barrier")   ? kSyncBarrier
+                    : !strcmp(sm, "stamped") ? kSyncStamped
+                    : !strcmp(sm, "gather")  ? kSyncGather
+                                             : kSyncAuto;
   // 512-thread CTAs (128 registers per thread) whenever the network fits in
   // one cell per thread at that size; 1024 threads for larger networks.
   // INFOLI_THREADS=512|1024 overrides.
@@ -347,7 +354,8 @@ int infoli_sim_create(const infoli_sim_desc* d, infoli_sim** out) {
       (rc = dev_upload(&s->d_edges, s->plan.edges.data(), s->plan.edges.size(), dv, st0)) ||
       (rc = dev_upload(&s->d_edge_g, s->plan.edge_g.data(), s->plan.edge_g.size(), dv, st0)) ||
       (rc = dev_upload(&s->d_probes, s->plan.probes.data(), s->plan.probes.size(), dv, st0)) ||
-      (rc = dev_upload(&s->d_gdesc, s->plan.gdesc.data(), s->plan.gdesc.size(), dv, st0)))
+      (rc = dev_upload(&s->d_gdesc, s->plan.gdesc.data(), s->plan.gdesc.size(), dv, st0)) ||
+      (rc = dev_upload(&s->d_gcol, s->plan.gcol.data(), s->plan.gcol.size(), dv, st0)))
     return fail(rc);
   // the kernel needs valid pointers even for empty tables
   if ((!s->d_chunks && pool_alloc(&s->d_chunks, sizeof(ChunkDesc), dv, st0) != cudaSuccess) ||
@@ -391,7 +399,8 @@ int infoli_sim_create(const infoli_sim_desc* d, infoli_sim** out) {
   s->dev_bytes = (int64_t)(pl.cta.size() * sizeof(CtaWork) + pl.tiles.size() * sizeof(TileDesc) +
                            pl.chunks.size() * sizeof(ChunkDesc) + pl.cell_slots.size() * sizeof(CellSlots) +
                            pl.edges.size() * sizeof(uint16_t) + pl.edge_g.size() * sizeof(float) +
-                           pl.probes.size() * sizeof(int) + pl.gdesc.size() * sizeof(int2_t)) +
+                           pl.probes.size() * sizeof(int) + pl.gdesc.size() * sizeof(int2_t) +
+                           pl.gcol.size() * sizeof(int32_t)) +
                  (int64_t)np * (2 * sizeof(float) + F_COUNT * sizeof(float) + sizeof(double)) + 256 +
                  (pl.shape.stamped ? (int64_t)np * 2 * sizeof(unsigned long long) : 0);
   *out = s;

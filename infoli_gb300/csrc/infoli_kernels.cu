@@ -721,6 +721,180 @@ __global__ void __launch_bounds__(BLOCK, 1) step_kernel(const __grid_constant__ 
   }
 }
 
+// Gather plans (sparse networks whose sender windows do not fit in shared
+// memory): one thread per receiver, state in registers, edges of a CTA's
+// receivers stored column by column (entry j of local receiver t at
+// base + j * n_cells + t, rows padded to the CTA's longest row with the
+// receiver itself, which adds exactly 0), so each load instruction of a warp
+// reads 32 consecutive entries; the senders' V_dend is read from the global
+// double buffer through L2.  One grid barrier per step.  Senders are summed in
+// the receiver's CSR order.
+template <int BLOCK, bool KAHAN, bool EDGE_G>
+__global__ void __launch_bounds__(BLOCK, 1) gather_kernel(const __grid_constant__ StepArgs a) {
+  __shared__ int s_abort;
+  const CtaWork w = a.cta[blockIdx.x];
+  const int tid = threadIdx.x;
+  const bool owner = tid < w.n_cells;
+  const int cell = w.cell_begin + tid;
+  const long long np = a.n_pad;
+  if (tid == 0) s_abort = 0;
+  Volts v{};
+  Gates g{};
+  float my_amp = 0.0f;
+  int my_onset = 0, my_off = 0;
+  if (owner) {
+    const float* st = a.st;
+    v.Vd = a.vd[a.step0 & 1][cell];
+    v.Vs = st[F_VS * np + cell];
+    v.Va = st[F_VA * np + cell];
+    g.q = st[F_Q * np + cell];
+    g.r = st[F_R * np + cell];
+    g.s = st[F_S * np + cell];
+    g.Ca = a.ca[cell];
+    g.ICaH = st[F_ICAH * np + cell];
+    g.gCaL = st[F_GCAL * np + cell];
+    g.k = st[F_K * np + cell];
+    g.l = st[F_L * np + cell];
+    g.m = st[F_M * np + cell];
+    g.h = st[F_H * np + cell];
+    g.n = st[F_N * np + cell];
+    g.p = st[F_P * np + cell];
+    g.xs = st[F_XS * np + cell];
+    g.ma = st[F_MA * np + cell];
+    g.ha = st[F_HA * np + cell];
+    g.xa = st[F_XA * np + cell];
+    if (a.stim_kind == STIM_CELL) {
+      my_amp = a.cell_amp[cell];
+      my_onset = a.cell_onset[cell];
+    }
+    if (a.cell_step_off) my_off = a.cell_step_off[cell];
+  }
+  const int deg = w.pad0;
+  const int stride = w.n_cells;
+  const int* __restrict__ ecol = a.gcol + (size_t)w.slot_begin + tid;
+  const float* __restrict__ eg = EDGE_G ? a.edge_g + (size_t)w.slot_begin + tid : nullptr;
+  const VoltCoef vk = volt_coef(a.P);
+  unsigned bar_target = 0;
+  int row = 0;
+  __syncthreads();
+  for (int t = 0; t < a.n_steps; ++t) {
+    const int step = a.step0 + t;
+    if (owner) {
+      const float* __restrict__ vcur = a.vd[step & 1];
+      const float vc = v.Vd;
+      float acc = 0.0f, comp = 0.0f;
+      int j = 0;
+      // four independent V_dend loads in flight per thread; the next group's
+      // sender ids are loaded while this group's V_dend loads are pending
+      int nidx[4];
+#pragma unroll
+      for (int u = 0; u < 4; ++u) nidx[u] = (u < deg) ? __ldg(ecol + (size_t)u * stride) : cell;
+      for (; j + 4 <= deg; j += 4) {
+        int sidx[4];
+        float gg[4], vs[4];
+#pragma unroll
+        for (int u = 0; u < 4; ++u) sidx[u] = nidx[u];
+#pragma unroll
+        for (int u = 0; u < 4; ++u) nidx[u] = (j + 4 + u < deg) ? __ldg(ecol + (size_t)(j + 4 + u) * stride) : cell;
+#pragma unroll
+        for (int u = 0; u < 4; ++u) {
+          vs[u] = __ldcg(vcur + sidx[u]);
+          gg[u] = EDGE_G ? __ldg(eg + (size_t)(j + u) * stride) : 1.0f;
+        }
+#pragma unroll
+        for (int u = 0; u < 4; ++u) {
+          const float V = vc - vs[u];
+          const float f = fmaf(0.8f, ex2_approx((V * V) * kNegLog2eOver100), 0.2f);
+          const float term = EDGE_G ? (gg[u] * f) * V : f * V;
+          if (KAHAN) {
+            const float y = term - comp;
+            const float s2 = acc + y;
+            comp = (s2 - acc) - y;
+            acc = s2;
+          } else {
+            acc += term;
+          }
+        }
+      }
+      for (; j < deg; ++j) {
+        const int sj = __ldg(ecol + (size_t)j * stride);
+        const float V = vc - __ldcg(vcur + sj);
+        const float f = fmaf(0.8f, ex2_approx((V * V) * kNegLog2eOver100), 0.2f);
+        const float term = EDGE_G ? (__ldg(eg + (size_t)j * stride) * f) * V : f * V;
+        if (KAHAN) {
+          const float y = term - comp;
+          const float s2 = acc + y;
+          comp = (s2 - acc) - y;
+          acc = s2;
+        } else {
+          acc += term;
+        }
+      }
+      const float ic = EDGE_G ? acc : acc * a.g_uniform;
+      const int ls = step + my_off;
+      float iapp;
+      if (a.stim_kind == STIM_PULSE)
+        iapp = (ls >= a.stim_start && ls < a.stim_end) ? a.stim_amp : 0.0f;
+      else if (a.stim_kind == STIM_CELL)
+        iapp = (ls >= my_onset && ls < my_onset + a.stim_dur) ? my_amp : 0.0f;
+      else
+        iapp = a.stim_table[(size_t)t * np + cell];
+      Currents cur;
+      run_units(a.P, 0xffu, v, g, cur);
+      voltage_step(a.P, vk, v, cur, ic, iapp);
+      a.vd[(step + 1) & 1][cell] = v.Vd;
+      if (a.trace_every > 0 && (step % a.trace_every) == 0) {
+        float* tr = a.trace + (size_t)row * a.trace_nq * np + cell;
+        int qi = 0;
+        if (a.trace_mask & TRACE_AXON) tr[(qi++) * np] = v.Va;
+        if (a.trace_mask & TRACE_SOMA) tr[(qi++) * np] = v.Vs;
+        if (a.trace_mask & TRACE_DEND) tr[(qi++) * np] = v.Vd;
+      }
+    }
+    if (a.trace_every > 0 && (step % a.trace_every) == 0) ++row;
+    if (t + 1 < a.n_steps) {
+      bar_target += gridDim.x;
+      if (!grid_sync(a, bar_target, &s_abort, nullptr)) break;
+    }
+  }
+  if (owner) {
+    float* st = a.st;
+    st[F_VS * np + cell] = v.Vs;
+    st[F_VA * np + cell] = v.Va;
+    st[F_Q * np + cell] = g.q;
+    st[F_R * np + cell] = g.r;
+    st[F_S * np + cell] = g.s;
+    a.ca[cell] = g.Ca;
+    st[F_ICAH * np + cell] = g.ICaH;
+    st[F_GCAL * np + cell] = g.gCaL;
+    st[F_K * np + cell] = g.k;
+    st[F_L * np + cell] = g.l;
+    st[F_M * np + cell] = g.m;
+    st[F_H * np + cell] = g.h;
+    st[F_N * np + cell] = g.n;
+    st[F_P * np + cell] = g.p;
+    st[F_XS * np + cell] = g.xs;
+    st[F_MA * np + cell] = g.ma;
+    st[F_HA * np + cell] = g.ha;
+    st[F_XA * np + cell] = g.xa;
+  }
+}
+
+template <int BLOCK, bool K, bool G>
+cudaError_t launch_gather(const StepArgs& a, int grid, cudaStream_t stream) {
+  void* args[] = {const_cast<StepArgs*>(&a)};
+  return cudaLaunchCooperativeKernel((const void*)gather_kernel<BLOCK, K, G>, dim3(grid), dim3(BLOCK), args, 0,
+                                     stream);
+}
+
+template <int BLOCK>
+cudaError_t launch_gather_block(const StepArgs& a, int grid, cudaStream_t stream) {
+  const bool g = a.edge_g != nullptr;
+  if (a.shape.kahan) return g ? launch_gather<BLOCK, true, true>(a, grid, stream)
+                              : launch_gather<BLOCK, true, false>(a, grid, stream);
+  return g ? launch_gather<BLOCK, false, true>(a, grid, stream) : launch_gather<BLOCK, false, false>(a, grid, stream);
+}
+
 template <int BLOCK, bool K, bool G, bool LL>
 cudaError_t launch_variant(const StepArgs& a, int grid, size_t smem, cudaStream_t stream) {
   auto fn = step_kernel<BLOCK, K, G, LL>;
@@ -750,8 +924,13 @@ cudaError_t launch_block(const StepArgs& a, int grid, size_t smem, cudaStream_t 
 size_t step_kernel_smem(const StepArgs& a) { return smem_layout(a.shape).total; }
 
 cudaError_t launch_step_kernel(const StepArgs& a, int grid, int threads, cudaStream_t stream) {
-  const size_t smem = step_kernel_smem(a);
   if (threads != a.shape.threads) return cudaErrorInvalidValue;
+  if (a.shape.gather) {
+    if (threads == 1024) return launch_gather_block<1024>(a, grid, stream);
+    if (threads == 512) return launch_gather_block<512>(a, grid, stream);
+    return cudaErrorInvalidValue;
+  }
+  const size_t smem = step_kernel_smem(a);
   if (threads == 1024) return launch_block<1024>(a, grid, smem, stream);
   if (threads == 512) return launch_block<512>(a, grid, smem, stream);
   return cudaErrorInvalidValue;

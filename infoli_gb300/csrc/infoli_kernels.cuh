@@ -38,6 +38,7 @@ struct StepArgs {
   const int2* cell_slots;     // per cell {slot_begin relative to CTA, slot_count}
   const uint16_t* edges;      // tile-relative sender offsets
   const float* edge_g;        // per-edge conductance (same order) or nullptr
+  const int* gcol;            // gather plans: sender ids, column by column per CTA
   const float* cell_g;        // per-cell conductance scale (uniform per network) or nullptr
   float g_uniform;            // used when edge_g and cell_g are both null
   // state

@@ -100,6 +100,9 @@ typedef struct {
   int dup_words;   // stamped: second copy of the window starts this many floats in
                    // (a multiple of 32 plus 16, so each word sits in two banks 16
                    // apart); 0 = single copy
+  int gather;      // gather plan: one thread per receiver reads its senders' V_dend
+                   // through L2; edges column by column per CTA (CtaWork::slot_begin
+                   // = first entry, pad0 = padded row length); no dynamic shared memory
 } SmemShape;
 
 // Number of per-cell float arrays kept in shared memory: V_dend, V_soma,

@@ -269,6 +269,68 @@ void pack_groups(Plan& P, const SmemLayout& L, const PlanInput& in, const std::v
 
 }  // namespace
 
+// Gather plan: cells partitioned over the CTAs by edge count (plus a per-cell
+// cost), each CTA's rows stored column by column and padded to its longest
+// row with the receiver itself (V = 0, so a pad adds exactly 0).
+static bool make_gather_plan(const PlanInput& in, Plan* out, std::string* err) {
+  const int n = in.n, threads = in.threads;
+  int grid = in.grid > 0 ? in.grid : in.grid_max;
+  grid = std::min(grid, in.grid_max);
+  grid = std::max(grid, (n + threads - 1) / threads);
+  if (grid > in.grid_max) {
+    *err = "make_plan: network larger than the co-resident thread count";
+    return false;
+  }
+  std::vector<int> starts = partition_cells(n, in.row_ptr, grid, threads);
+  const int ctas = (int)starts.size() - 1;
+  Plan& P = *out;
+  P = Plan();
+  P.grid = ctas;
+  P.threads = threads;
+  P.cta.resize(ctas);
+  int64_t total = 0;
+  int cells_cap = 32;
+  for (int b = 0; b < ctas; ++b) {
+    int deg = 0;
+    for (int c = starts[b]; c < starts[b + 1]; ++c) deg = std::max<int>(deg, (int)(in.row_ptr[c + 1] - in.row_ptr[c]));
+    CtaWork& w = P.cta[b];
+    w = CtaWork{};
+    w.cell_begin = starts[b];
+    w.n_cells = starts[b + 1] - starts[b];
+    w.slot_begin = (int)std::min<int64_t>(total, INT32_MAX);
+    w.pad0 = deg;
+    total += (int64_t)deg * w.n_cells;
+    cells_cap = std::max(cells_cap, ((w.n_cells + 31) / 32) * 32);
+  }
+  if (total > INT32_MAX) {
+    *err = "make_plan: gather plan needs more than 2^31-1 entries";
+    return false;
+  }
+  P.gcol.assign((size_t)total, 0);
+  if (in.g) P.edge_g.assign((size_t)total, 0.0f);
+  for (int b = 0; b < ctas; ++b) {
+    const CtaWork& w = P.cta[b];
+    for (int t = 0; t < w.n_cells; ++t) {
+      const int c = w.cell_begin + t;
+      const int64_t e0 = in.row_ptr[c], len = in.row_ptr[c + 1] - e0;
+      for (int j = 0; j < w.pad0; ++j) {
+        const size_t at = (size_t)w.slot_begin + (size_t)j * w.n_cells + t;
+        P.gcol[at] = j < len ? in.col[e0 + j] : c;
+        if (in.g) P.edge_g[at] = j < len ? in.g[e0 + j] : 0.0f;
+      }
+    }
+  }
+  P.cell_slots.assign(n, CellSlots{0, 0});
+  P.shape = SmemShape{};
+  P.shape.threads = threads;
+  P.shape.cells_cap = cells_cap;
+  P.shape.kahan = in.kahan;
+  P.shape.edge_g = in.g != nullptr;
+  P.shape.gather = 1;
+  P.smem_bytes = 0;
+  return true;
+}
+
 bool make_plan(const PlanInput& in, Plan* out, std::string* err) {
   const int n = in.n;
   if (n <= 0 || !in.row_ptr || in.threads <= 0 || in.threads % 32 || in.grid_max <= 0) {
@@ -296,6 +358,7 @@ bool make_plan(const PlanInput& in, Plan* out, std::string* err) {
     *err = "make_plan: more than 2^31-1 edges";
     return false;
   }
+  if (in.sync_mode == kSyncGather) return make_gather_plan(in, out, err);
   const int threads = in.threads;
   const int nwarps = threads / 32;
   const int n_pad = pad_cells(n);
@@ -569,6 +632,10 @@ bool make_plan(const PlanInput& in, Plan* out, std::string* err) {
   }
   P.shape = sh;
   P.smem_bytes = smem_layout(sh).total;
+  // windows larger than shared memory and short rows: gather through L2
+  // instead of staging tiles (each row would be cut into a few edges per tile)
+  if (!sh.stamped && in.sync_mode == kSyncAuto && E <= (int64_t)kGatherMaxMeanDegree * n)
+    return make_gather_plan(in, out, err);
   return true;
 }
 
@@ -605,6 +672,22 @@ extern "C" int infoli_plan_emulate(int n, const int64_t* row_ptr, const int32_t*
   int64_t groups = 0, probes = 0, gather_waves = 0, gathers = 0;
   for (const CtaWork& w : P.cta) {
     if (w.n_cells > threads || w.n_cells > P.shape.cells_cap) return -3;
+    if (P.shape.gather) {
+      for (int t = 0; t < w.n_cells; ++t) {
+        const int c = w.cell_begin + t;
+        float acc = 0.0f;
+        for (int j = 0; j < w.pad0; ++j) {
+          const size_t at = (size_t)w.slot_begin + (size_t)j * w.n_cells + t;
+          if (at >= P.gcol.size()) return -8;
+          const int s = P.gcol[at];
+          if (s < 0 || s >= n) return -7;
+          const float V = vdend[c] - vdend[s];
+          acc += (g ? P.edge_g[at] : 1.0f) * fexp(V) * V;
+        }
+        ic_out[c] = g ? acc : acc * g_uniform;
+      }
+      continue;
+    }
     std::fill(sm.begin(), sm.end(), 0);
     float* fsm = reinterpret_cast<float*>(sm.data());
     std::vector<float> part(P.shape.max_slots, 0.0f);
@@ -690,7 +773,7 @@ extern "C" int infoli_plan_emulate(int n, const int64_t* row_ptr, const int32_t*
   }
   if (info) {
     info[0] = P.grid;
-    info[1] = P.shape.stamped;
+    info[1] = P.shape.gather ? 2 : P.shape.stamped;
     info[2] = (int64_t)P.tiles.size();
     info[3] = P.shape.stamped ? groups : (int64_t)P.chunks.size();
     info[4] = P.shape.max_slots;

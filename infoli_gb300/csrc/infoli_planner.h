@@ -37,7 +37,11 @@ struct PlanInput {
   int sync_mode = 0;               // kSyncAuto / kSyncBarrier / kSyncStamped
 };
 
-enum { kSyncAuto = 0, kSyncBarrier = 1, kSyncStamped = 2 };
+enum { kSyncAuto = 0, kSyncBarrier = 1, kSyncStamped = 2, kSyncGather = 3 };
+
+// Auto mode picks a gather plan over a barrier plan when the mean degree is
+// at most this (rows too short to fill a warp per chunk once split by tiles).
+enum { kGatherMaxMeanDegree = 384 };
 
 struct Plan {
   int grid = 0, threads = 0, tile_cap = 0, nbuf = 1, max_slots = 0;
@@ -51,6 +55,7 @@ struct Plan {
   std::vector<float> edge_g;          // empty unless per-edge g
   std::vector<int> probes;            // stamped mode: progress-probe cells
   std::vector<int2_t> gdesc;          // stamped mode: {slot, recv} per lane-chunk, 32 per group
+  std::vector<int32_t> gcol;          // gather mode: sender ids, column by column per CTA
 };
 
 // Shared-memory bytes the step kernel needs for a plan's parameters.

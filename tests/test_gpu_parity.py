@@ -103,14 +103,15 @@ def test_grid_gaussian_multi_cta(ig, conf):
     assert np.max(np.abs(gpu["soma"] - ref["soma"])) <= TOL_VSOMA_MV
 
 
-@pytest.mark.parametrize("kahan", [False, True])
-def test_per_edge_g_and_cell_pulses_spike_times(ig, conf, kahan):
+@pytest.mark.parametrize("kahan,mode", [(False, "auto"), (True, "auto"), (True, "gather")])
+def test_per_edge_g_and_cell_pulses_spike_times(ig, conf, kahan, mode, monkeypatch):
     """CSR with per-edge g ~ U(0.02,0.06), per-cell 5 ms pulses: V_soma over the
     first 2000 steps (before any pulse) and soma spike steps over 1 s.  Onsets are
     U(100, 1000) ms so the first 2000 steps stay subthreshold; amplitudes U(10,14)
     make about a third of the cells spike (U(0,8) does not reach threshold in 5 ms,
     and much stronger pulses drive the explicit-Euler model to overflow, as in the
     reference)."""
+    monkeypatch.setenv("INFOLI_SYNC", mode)
     n, k = 600, 30
     rp, col, g = ig.gen_fixed_degree(n, k, 4, (0.02, 0.06))
     rng = np.random.default_rng(8)
@@ -125,23 +126,28 @@ def test_per_edge_g_and_cell_pulses_spike_times(ig, conf, kahan):
     assert spikes_match(sg, sr)
 
 
-def test_many_tiles_path(ig, conf):
-    """A sender window larger than one shared-memory tile (several staged tiles per CTA)."""
+@pytest.mark.parametrize("mode", ["barrier", "gather"])
+def test_large_window_paths(ig, conf, mode, monkeypatch):
+    """A sender window larger than shared memory: several staged tiles per CTA
+    (barrier) or senders read through L2 (gather, the default for short rows)."""
+    monkeypatch.setenv("INFOLI_SYNC", mode)
     n, k = 90000, 6
     rp, col, g = ig.gen_fixed_degree(n, k, 12, (0.02, 0.06))
     st0 = hetero_state(conf, n, 7)
     sim = ig.Simulation(n, conf, rp, col, g=g, init_state=st0)
     info = sim.plan_info()
     sim.close()
-    assert info["tiles"] > info["grid"]
+    if mode == "barrier":
+        assert info["tiles"] > info["grid"]
     gpu, ref, _, _ = _compare(ig, conf, n, rp, col, st0, steps=300, g=g, nthreads=16)
     assert np.max(np.abs(gpu["soma"] - ref["soma"])) <= TOL_VSOMA_MV
 
 
-@pytest.mark.parametrize("mode", ["barrier", "stamped"])
+@pytest.mark.parametrize("mode", ["barrier", "stamped", "gather"])
 def test_exchange_modes_match_oracle(ig, conf, mode, monkeypatch):
-    """Both V_dend exchanges (grid barrier + bulk tiles; stamped words) on a
-    multi-CTA grid network; each is deterministic run to run."""
+    """Every V_dend exchange (grid barrier + bulk tiles; stamped words; grid
+    barrier + L2 gathers) on a multi-CTA grid network; each is deterministic
+    run to run."""
     monkeypatch.setenv("INFOLI_SYNC", mode)
     rp, col = ig.gen_grid_gaussian(40, 50, 6.0, 10.0, 3)
     n = 2000
