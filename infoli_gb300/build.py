@@ -70,7 +70,7 @@ def build(verbose: bool = False, force: bool = False) -> str:
         obj = os.path.join(OUT, f + ".o")
         objs.append(obj)
         if force or _stale(obj, [src] + headers):
-            jobs.append(["g++", "-O3", "-std=c++17", "-fPIC", "-Wall", "-I", INC, "-c", src, "-o", obj])
+            jobs.append(["g++", "-O3", "-std=c++17", "-fPIC", "-Wall", "-fopenmp", "-I", INC, "-c", src, "-o", obj])
     for f in C_SOURCES:
         src = os.path.join(SRC, f)
         obj = os.path.join(OUT, f + ".o")

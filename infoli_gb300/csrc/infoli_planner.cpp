@@ -383,8 +383,10 @@ bool make_plan(const PlanInput& in, Plan* out, std::string* err) {
   // ---- per-CTA sorted edges (sender, g) and unique sender lists
   std::vector<std::vector<int>> uniq(ctas);
   int max_window = 4;
+#pragma omp parallel for schedule(dynamic, 1) reduction(max : max_window)
   for (int b = 0; b < ctas; ++b) {
     std::vector<int>& u = uniq[b];
+    u.reserve((size_t)(in.row_ptr[starts[b + 1]] - in.row_ptr[starts[b]]));
     for (int c = starts[b]; c < starts[b + 1]; ++c)
       for (int64_t e = in.row_ptr[c]; e < in.row_ptr[c + 1]; ++e) u.push_back(in.col[e]);
     std::sort(u.begin(), u.end());
@@ -422,6 +424,7 @@ bool make_plan(const PlanInput& in, Plan* out, std::string* err) {
   for (int attempt = 0; attempt < 32; ++attempt) {
     if (max_window > tile_cap) nbuf = 2;
     max_slots = 0;
+#pragma omp parallel for schedule(dynamic, 1) reduction(max : max_slots)
     for (int b = 0; b < ctas; ++b) {
       tiles[b] = make_tiles(uniq[b], tile_cap, n_pad);
       max_slots = std::max(max_slots, slots_for(b, tiles[b]));
@@ -461,76 +464,105 @@ bool make_plan(const PlanInput& in, Plan* out, std::string* err) {
   P.max_slots = max_slots;
   P.smem_bytes = plan_smem_bytes(tile_cap, nbuf, threads, cells_cap, max_slots, in.kahan);
   P.cell_slots.assign(n, CellSlots{0, 0});
-  P.edges.reserve(E);
-  if (in.g) P.edge_g.reserve(E);
-  int slot_base = 0;
-  struct PendingChunk {
-    int tile, recv, slot;
-    std::vector<std::pair<int, float>> e;  // (sender, g)
+  // Each CTA's tables are built on their own (in parallel, indices local to
+  // the CTA), then concatenated in CTA order with their offsets applied.
+  struct Local {
+    std::vector<TileDesc> tiles;
+    std::vector<ChunkDesc> chunks;
+    std::vector<uint16_t> edges;
+    std::vector<float> edge_g;
+    int n_slots = 0;
   };
+  std::vector<Local> loc(ctas);
+#pragma omp parallel for schedule(dynamic, 1)
   for (int b = 0; b < ctas; ++b) {
-    CtaWork w{};
-    w.cell_begin = starts[b];
-    w.n_cells = starts[b + 1] - starts[b];
-    w.tile_begin = (int)P.tiles.size();
-    w.n_tiles = (int)tiles[b].size();
-    w.slot_begin = slot_base;
+    Local& L = loc[b];
     const std::vector<TileSpan>& tl = tiles[b];
-    std::vector<PendingChunk> pend;
+    // senders of the CTA's cells, each cell's sorted by id, end to end
+    std::vector<std::pair<int, float>> snd;
+    snd.reserve((size_t)(in.row_ptr[starts[b + 1]] - in.row_ptr[starts[b]]));
+    struct Pending {
+      int tile, recv, slot;
+      size_t begin, count;  // range in snd
+    };
+    std::vector<Pending> pend;
     int slot = 0;
-    for (int r = 0; r < w.n_cells; ++r) {
-      const int c = w.cell_begin + r;
-      std::vector<std::pair<int, float>> snd;
-      for (int64_t e = in.row_ptr[c]; e < in.row_ptr[c + 1]; ++e)
-        snd.push_back({in.col[e], in.g ? in.g[e] : 0.0f});
-      std::stable_sort(snd.begin(), snd.end(),
+    for (int c = starts[b]; c < starts[b + 1]; ++c) {
+      const int r = c - starts[b];
+      const size_t s0 = snd.size();
+      for (int64_t e = in.row_ptr[c]; e < in.row_ptr[c + 1]; ++e) snd.push_back({in.col[e], in.g ? in.g[e] : 0.0f});
+      std::stable_sort(snd.begin() + s0, snd.end(),
                        [](const std::pair<int, float>& x, const std::pair<int, float>& y) { return x.first < y.first; });
       P.cell_slots[c].begin = slot;
-      size_t k = 0;
+      size_t k = s0;
       for (int j = 0; j < (int)tl.size(); ++j) {
-        std::vector<std::pair<int, float>> in_tile;
-        while (k < snd.size() && snd[k].first < tl[j].hi) in_tile.push_back(snd[k++]);
-        for (size_t o = 0; o < in_tile.size(); o += chunk) {
-          PendingChunk pc;
-          pc.tile = j;
-          pc.recv = r;
-          pc.slot = slot++;
-          pc.e.assign(in_tile.begin() + o, in_tile.begin() + std::min(in_tile.size(), o + (size_t)chunk));
-          pend.push_back(std::move(pc));
-        }
+        const size_t t0 = k;
+        while (k < snd.size() && snd[k].first < tl[j].hi) ++k;
+        for (size_t o = t0; o < k; o += chunk) pend.push_back({j, r, slot++, o, std::min(k - o, (size_t)chunk)});
       }
       P.cell_slots[c].count = slot - P.cell_slots[c].begin;
     }
-    w.n_slots = slot;
+    L.n_slots = slot;
     // tile-major; inside a tile, larger chunks first (round-robin to warps)
-    std::stable_sort(pend.begin(), pend.end(), [](const PendingChunk& x, const PendingChunk& y) {
+    std::stable_sort(pend.begin(), pend.end(), [](const Pending& x, const Pending& y) {
       if (x.tile != y.tile) return x.tile < y.tile;
-      return x.e.size() > y.e.size();
+      return x.count > y.count;
     });
+    L.edges.reserve(snd.size());
+    if (in.g) L.edge_g.reserve(snd.size());
     size_t pi = 0;
     for (int j = 0; j < (int)tl.size(); ++j) {
       TileDesc td{};
       td.lo = tl[j].lo;
       td.nfloats = tl[j].hi - tl[j].lo;
-      td.chunk_begin = (int)P.chunks.size();
+      td.chunk_begin = (int)L.chunks.size();
       while (pi < pend.size() && pend[pi].tile == j) {
-        const PendingChunk& pc = pend[pi++];
+        const Pending& pc = pend[pi++];
         ChunkDesc cd{};
-        cd.edge_begin = (int)P.edges.size();
+        cd.edge_begin = (int)L.edges.size();
         cd.slot = pc.slot;
         cd.recv = pc.recv;
-        cd.count = (int)pc.e.size();
-        for (const auto& se : pc.e) {
-          P.edges.push_back((uint16_t)(se.first - td.lo));
-          if (in.g) P.edge_g.push_back(se.second);
+        cd.count = (int)pc.count;
+        for (size_t q = pc.begin; q < pc.begin + pc.count; ++q) {
+          L.edges.push_back((uint16_t)(snd[q].first - td.lo));
+          if (in.g) L.edge_g.push_back(snd[q].second);
         }
-        P.chunks.push_back(cd);
+        L.chunks.push_back(cd);
       }
-      td.chunk_end = (int)P.chunks.size();
+      td.chunk_end = (int)L.chunks.size();
+      L.tiles.push_back(td);
+    }
+  }
+  P.edges.reserve(E);
+  if (in.g) P.edge_g.reserve(E);
+  int slot_base = 0;
+  for (int b = 0; b < ctas; ++b) {
+    Local& L = loc[b];
+    CtaWork w{};
+    w.cell_begin = starts[b];
+    w.n_cells = starts[b + 1] - starts[b];
+    w.tile_begin = (int)P.tiles.size();
+    w.n_tiles = (int)L.tiles.size();
+    w.slot_begin = slot_base;
+    w.n_slots = L.n_slots;
+    const int chunk0 = (int)P.chunks.size(), edge0 = (int)P.edges.size();
+    for (TileDesc td : L.tiles) {
+      td.chunk_begin += chunk0;
+      td.chunk_end += chunk0;
       P.tiles.push_back(td);
     }
-    slot_base += slot;
+    for (ChunkDesc cd : L.chunks) {
+      cd.edge_begin += edge0;
+      P.chunks.push_back(cd);
+    }
+    P.edges.insert(P.edges.end(), L.edges.begin(), L.edges.end());
+    if (in.g) P.edge_g.insert(P.edge_g.end(), L.edge_g.begin(), L.edge_g.end());
+    slot_base += L.n_slots;
     P.cta.push_back(w);
+    std::vector<TileDesc>().swap(L.tiles);
+    std::vector<ChunkDesc>().swap(L.chunks);
+    std::vector<uint16_t>().swap(L.edges);
+    std::vector<float>().swap(L.edge_g);
   }
 
   // ---- shared-memory shape; keep the static work resident when it fits
