@@ -322,6 +322,7 @@ int infoli_sim_create(const infoli_sim_desc* d, infoli_sim** out) {
     pin.sync_mode = !strcmp(sm, "barrier")   ? kSyncBarrier
                     : !strcmp(sm, "stamped") ? kSyncStamped
                     : !strcmp(sm, "gather")  ? kSyncGather
+                    : !strcmp(sm, "tgather") ? kSyncTiledGather
                                              : kSyncAuto;
   // 512-thread CTAs (128 registers per thread) whenever the network fits in
   // one cell per thread at that size; 1024 threads for larger networks.

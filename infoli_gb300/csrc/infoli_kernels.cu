@@ -729,8 +729,56 @@ __global__ void __launch_bounds__(BLOCK, 1) step_kernel(const __grid_constant__ 
 // reads 32 consecutive entries; the senders' V_dend is read from the global
 // double buffer through L2.  One grid barrier per step.  Senders are summed in
 // the receiver's CSR order.
+// Gate state of the gather kernel in shared memory (15 floats + FP64 Ca2+ per
+// cell), so the coupling loop has the registers for many loads in flight.
+constexpr int kGatherGateFloats = 15;
+constexpr int kGatherGroup = 8;  // V_dend loads in flight per thread
+
+__device__ __forceinline__ void gather_store_gates(float* sg, double* sca, int blk, int t, const Gates& g) {
+  const float f[kGatherGateFloats] = {g.q, g.r, g.s, g.ICaH, g.gCaL, g.k, g.l, g.m,
+                                      g.h, g.n, g.p, g.xs, g.ma, g.ha, g.xa};
+#pragma unroll
+  for (int i = 0; i < kGatherGateFloats; ++i) sg[i * blk + t] = f[i];
+  sca[t] = g.Ca;
+}
+
+__device__ __forceinline__ Gates gather_load_gates(const float* sg, const double* sca, int blk, int t) {
+  Gates g;
+  g.q = sg[0 * blk + t];
+  g.r = sg[1 * blk + t];
+  g.s = sg[2 * blk + t];
+  g.ICaH = sg[3 * blk + t];
+  g.gCaL = sg[4 * blk + t];
+  g.k = sg[5 * blk + t];
+  g.l = sg[6 * blk + t];
+  g.m = sg[7 * blk + t];
+  g.h = sg[8 * blk + t];
+  g.n = sg[9 * blk + t];
+  g.p = sg[10 * blk + t];
+  g.xs = sg[11 * blk + t];
+  g.ma = sg[12 * blk + t];
+  g.ha = sg[13 * blk + t];
+  g.xa = sg[14 * blk + t];
+  g.Ca = sca[t];
+  return g;
+}
+
+size_t gather_smem_bytes(int block) { return (size_t)block * (kGatherGateFloats * sizeof(float) + sizeof(double)); }
+
+// Gather plans (sparse networks whose sender windows do not fit in shared
+// memory): one thread per receiver, voltages in registers and gate state in
+// shared memory; edges of a CTA's receivers stored column by column (entry j
+// of local receiver t at base + j * n_cells + t, rows padded to the CTA's
+// longest row with the receiver itself, which adds exactly 0), so each load
+// instruction of a warp reads 32 consecutive entries; the senders' V_dend is
+// read from the global double buffer through L2, kGatherGroup loads in flight
+// per thread with the next group's sender ids already loaded.  One grid
+// barrier per step.  Senders are summed in the receiver's CSR order.
 template <int BLOCK, bool KAHAN, bool EDGE_G>
 __global__ void __launch_bounds__(BLOCK, 1) gather_kernel(const __grid_constant__ StepArgs a) {
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  double* sCa = reinterpret_cast<double*>(smem_raw);
+  float* sGt = reinterpret_cast<float*>(smem_raw + sizeof(double) * BLOCK);
   __shared__ int s_abort;
   const CtaWork w = a.cta[blockIdx.x];
   const int tid = threadIdx.x;
@@ -738,6 +786,162 @@ __global__ void __launch_bounds__(BLOCK, 1) gather_kernel(const __grid_constant_
   const int cell = w.cell_begin + tid;
   const long long np = a.n_pad;
   if (tid == 0) s_abort = 0;
+  Volts v{};
+  float my_amp = 0.0f;
+  int my_onset = 0, my_off = 0;
+  if (owner) {
+    const float* st = a.st;
+    v.Vd = a.vd[a.step0 & 1][cell];
+    v.Vs = st[F_VS * np + cell];
+    v.Va = st[F_VA * np + cell];
+    Gates g;
+    g.q = st[F_Q * np + cell];
+    g.r = st[F_R * np + cell];
+    g.s = st[F_S * np + cell];
+    g.Ca = a.ca[cell];
+    g.ICaH = st[F_ICAH * np + cell];
+    g.gCaL = st[F_GCAL * np + cell];
+    g.k = st[F_K * np + cell];
+    g.l = st[F_L * np + cell];
+    g.m = st[F_M * np + cell];
+    g.h = st[F_H * np + cell];
+    g.n = st[F_N * np + cell];
+    g.p = st[F_P * np + cell];
+    g.xs = st[F_XS * np + cell];
+    g.ma = st[F_MA * np + cell];
+    g.ha = st[F_HA * np + cell];
+    g.xa = st[F_XA * np + cell];
+    gather_store_gates(sGt, sCa, BLOCK, tid, g);
+    if (a.stim_kind == STIM_CELL) {
+      my_amp = a.cell_amp[cell];
+      my_onset = a.cell_onset[cell];
+    }
+    if (a.cell_step_off) my_off = a.cell_step_off[cell];
+  }
+  const int deg = w.pad0;
+  const int stride = w.n_cells;
+  const int* __restrict__ ecol = a.gcol + (size_t)w.slot_begin + tid;
+  const float* __restrict__ eg = EDGE_G ? a.edge_g + (size_t)w.slot_begin + tid : nullptr;
+  const VoltCoef vk = volt_coef(a.P);
+  unsigned bar_target = 0;
+  int row = 0;
+  __syncthreads();
+  for (int t = 0; t < a.n_steps; ++t) {
+    const int step = a.step0 + t;
+    if (owner) {
+      const float* __restrict__ vcur = a.vd[step & 1];
+      const float vc = v.Vd;
+      float acc = 0.0f, comp = 0.0f;
+      int nidx[kGatherGroup];
+#pragma unroll
+      for (int u = 0; u < kGatherGroup; ++u) nidx[u] = (u < deg) ? __ldg(ecol + (size_t)u * stride) : cell;
+      for (int j = 0; j < deg; j += kGatherGroup) {
+        float vs[kGatherGroup], gg[kGatherGroup];
+#pragma unroll
+        for (int u = 0; u < kGatherGroup; ++u) {
+          vs[u] = __ldcg(vcur + nidx[u]);  // past the row end: the receiver itself
+          gg[u] = (EDGE_G && j + u < deg) ? __ldg(eg + (size_t)(j + u) * stride) : 0.0f;
+        }
+#pragma unroll
+        for (int u = 0; u < kGatherGroup; ++u) {
+          const int jn = j + kGatherGroup + u;
+          nidx[u] = (jn < deg) ? __ldg(ecol + (size_t)jn * stride) : cell;
+        }
+#pragma unroll
+        for (int u = 0; u < kGatherGroup; ++u) {
+          const float V = vc - vs[u];
+          const float f = fmaf(0.8f, ex2_approx((V * V) * kNegLog2eOver100), 0.2f);
+          const float term = EDGE_G ? (gg[u] * f) * V : f * V;
+          if (KAHAN) {
+            const float y = term - comp;
+            const float s2 = acc + y;
+            comp = (s2 - acc) - y;
+            acc = s2;
+          } else {
+            acc += term;
+          }
+        }
+      }
+      const float ic = EDGE_G ? acc : acc * a.g_uniform;
+      const int ls = step + my_off;
+      float iapp;
+      if (a.stim_kind == STIM_PULSE)
+        iapp = (ls >= a.stim_start && ls < a.stim_end) ? a.stim_amp : 0.0f;
+      else if (a.stim_kind == STIM_CELL)
+        iapp = (ls >= my_onset && ls < my_onset + a.stim_dur) ? my_amp : 0.0f;
+      else
+        iapp = a.stim_table[(size_t)t * np + cell];
+      Gates g = gather_load_gates(sGt, sCa, BLOCK, tid);
+      Currents cur;
+      run_units(a.P, 0xffu, v, g, cur);
+      voltage_step(a.P, vk, v, cur, ic, iapp);
+      gather_store_gates(sGt, sCa, BLOCK, tid, g);
+      a.vd[(step + 1) & 1][cell] = v.Vd;
+      if (a.trace_every > 0 && (step % a.trace_every) == 0) {
+        float* tr = a.trace + (size_t)row * a.trace_nq * np + cell;
+        int qi = 0;
+        if (a.trace_mask & TRACE_AXON) tr[(qi++) * np] = v.Va;
+        if (a.trace_mask & TRACE_SOMA) tr[(qi++) * np] = v.Vs;
+        if (a.trace_mask & TRACE_DEND) tr[(qi++) * np] = v.Vd;
+      }
+    }
+    if (a.trace_every > 0 && (step % a.trace_every) == 0) ++row;
+    if (t + 1 < a.n_steps) {
+      bar_target += gridDim.x;
+      if (!grid_sync(a, bar_target, &s_abort, nullptr)) break;
+    }
+  }
+  if (owner) {
+    const Gates g = gather_load_gates(sGt, sCa, BLOCK, tid);
+    float* st = a.st;
+    st[F_VS * np + cell] = v.Vs;
+    st[F_VA * np + cell] = v.Va;
+    st[F_Q * np + cell] = g.q;
+    st[F_R * np + cell] = g.r;
+    st[F_S * np + cell] = g.s;
+    a.ca[cell] = g.Ca;
+    st[F_ICAH * np + cell] = g.ICaH;
+    st[F_GCAL * np + cell] = g.gCaL;
+    st[F_K * np + cell] = g.k;
+    st[F_L * np + cell] = g.l;
+    st[F_M * np + cell] = g.m;
+    st[F_H * np + cell] = g.h;
+    st[F_N * np + cell] = g.n;
+    st[F_P * np + cell] = g.p;
+    st[F_XS * np + cell] = g.xs;
+    st[F_MA * np + cell] = g.ma;
+    st[F_HA * np + cell] = g.ha;
+    st[F_XA * np + cell] = g.xa;
+  }
+}
+
+// Tiled gather plans: one thread per receiver with its state in registers;
+// each step the CTA's tiles of V_dend are staged into shared memory by bulk
+// async copies (two buffers when there are several tiles: the next tile's
+// copy overlaps this tile's gathers) and every receiver walks its senders in
+// the tile (16-bit offsets, column by column, its own count).  One grid
+// barrier per step; senders are summed tile by tile in ascending order.
+template <int BLOCK, bool KAHAN, bool EDGE_G>
+__global__ void __launch_bounds__(BLOCK, 1) tgather_kernel(const __grid_constant__ StepArgs a) {
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  __shared__ int s_abort;
+  float* tbuf = reinterpret_cast<float*>(smem_raw);
+  const int tile_cap = a.shape.tile_cap, nbuf = a.shape.nbuf;
+  uint64_t* mbar = reinterpret_cast<uint64_t*>(
+      smem_raw + (((size_t)nbuf * (size_t)tile_cap * sizeof(float) + 15) & ~(size_t)15));
+  const CtaWork w = a.cta[blockIdx.x];
+  const TileDesc* tiles = a.tiles + w.tile_begin;
+  const int tid = threadIdx.x;
+  const bool owner = tid < w.n_cells;
+  const int cell = w.cell_begin + tid;
+  const long long np = a.n_pad;
+  const int nc = w.n_cells;
+  if (tid == 0) {
+    mbar_init(&mbar[0], 1);
+    mbar_init(&mbar[1], 1);
+    fence_mbar_init();
+    s_abort = 0;
+  }
   Volts v{};
   Gates g{};
   float my_amp = 0.0f;
@@ -769,43 +973,45 @@ __global__ void __launch_bounds__(BLOCK, 1) gather_kernel(const __grid_constant_
     }
     if (a.cell_step_off) my_off = a.cell_step_off[cell];
   }
-  const int deg = w.pad0;
-  const int stride = w.n_cells;
-  const int* __restrict__ ecol = a.gcol + (size_t)w.slot_begin + tid;
-  const float* __restrict__ eg = EDGE_G ? a.edge_g + (size_t)w.slot_begin + tid : nullptr;
+  const int* __restrict__ counts = a.gcol + (size_t)w.slot_begin + tid;
   const VoltCoef vk = volt_coef(a.P);
-  unsigned bar_target = 0;
+  unsigned bar_target = 0, nload = 0;
   int row = 0;
   __syncthreads();
   for (int t = 0; t < a.n_steps; ++t) {
     const int step = a.step0 + t;
-    if (owner) {
-      const float* __restrict__ vcur = a.vd[step & 1];
-      const float vc = v.Vd;
-      float acc = 0.0f, comp = 0.0f;
-      int j = 0;
-      // four independent V_dend loads in flight per thread; the next group's
-      // sender ids are loaded while this group's V_dend loads are pending
-      int nidx[4];
-#pragma unroll
-      for (int u = 0; u < 4; ++u) nidx[u] = (u < deg) ? __ldg(ecol + (size_t)u * stride) : cell;
-      for (; j + 4 <= deg; j += 4) {
-        int sidx[4];
-        float gg[4], vs[4];
-#pragma unroll
-        for (int u = 0; u < 4; ++u) sidx[u] = nidx[u];
-#pragma unroll
-        for (int u = 0; u < 4; ++u) nidx[u] = (j + 4 + u < deg) ? __ldg(ecol + (size_t)(j + 4 + u) * stride) : cell;
-#pragma unroll
-        for (int u = 0; u < 4; ++u) {
-          vs[u] = __ldcg(vcur + sidx[u]);
-          gg[u] = EDGE_G ? __ldg(eg + (size_t)(j + u) * stride) : 1.0f;
-        }
-#pragma unroll
-        for (int u = 0; u < 4; ++u) {
-          const float V = vc - vs[u];
+    const float* vcur = a.vd[step & 1];
+    float acc = 0.0f, comp = 0.0f;
+    if (w.n_tiles > 0 && tid == 0) {
+      fence_proxy_async_global();
+      fence_proxy_async_smem();
+      issue_tile(a, vcur, tiles[0], tbuf + (nload % nbuf) * tile_cap, &mbar[nload % nbuf]);
+    }
+    for (int j = 0; j < w.n_tiles; ++j) {
+      const TileDesc td = tiles[j];
+      const unsigned k = nload + j;
+      const int b = (int)(k % (unsigned)nbuf);
+      const float* buf = tbuf + b * tile_cap;
+      if (tid == 0 && j > 0 && nbuf == 1) {
+        fence_proxy_async_smem();
+        issue_tile(a, vcur, td, tbuf, &mbar[0]);
+      }
+      if (tid == 0 && j + 1 < w.n_tiles && nbuf == 2) {
+        fence_proxy_async_smem();
+        const int b1 = (int)((k + 1) & 1u);
+        issue_tile(a, vcur, tiles[j + 1], tbuf + b1 * tile_cap, &mbar[b1]);
+      }
+      const int cnt = owner ? __ldg(counts + (size_t)j * nc) : 0;
+      if (!wait_tile(a, &mbar[b], (k / (unsigned)nbuf) & 1u)) s_abort = 1;
+      if (owner) {
+        const uint16_t* __restrict__ ent = a.edges + (size_t)td.chunk_begin + tid;
+        const float* __restrict__ eg = EDGE_G ? a.edge_g + (size_t)td.chunk_begin + tid : nullptr;
+        const float vc = v.Vd;
+#pragma unroll 4
+        for (int q = 0; q < cnt; ++q) {
+          const float V = vc - buf[__ldg(ent + (size_t)q * nc)];
           const float f = fmaf(0.8f, ex2_approx((V * V) * kNegLog2eOver100), 0.2f);
-          const float term = EDGE_G ? (gg[u] * f) * V : f * V;
+          const float term = EDGE_G ? (__ldg(eg + (size_t)q * nc) * f) * V : f * V;
           if (KAHAN) {
             const float y = term - comp;
             const float s2 = acc + y;
@@ -816,20 +1022,11 @@ __global__ void __launch_bounds__(BLOCK, 1) gather_kernel(const __grid_constant_
           }
         }
       }
-      for (; j < deg; ++j) {
-        const int sj = __ldg(ecol + (size_t)j * stride);
-        const float V = vc - __ldcg(vcur + sj);
-        const float f = fmaf(0.8f, ex2_approx((V * V) * kNegLog2eOver100), 0.2f);
-        const float term = EDGE_G ? (__ldg(eg + (size_t)j * stride) * f) * V : f * V;
-        if (KAHAN) {
-          const float y = term - comp;
-          const float s2 = acc + y;
-          comp = (s2 - acc) - y;
-          acc = s2;
-        } else {
-          acc += term;
-        }
-      }
+      __syncthreads();  // every thread is done with this buffer before it is refilled
+    }
+    nload += w.n_tiles;
+    if (s_abort) break;
+    if (owner) {
       const float ic = EDGE_G ? acc : acc * a.g_uniform;
       const int ls = step + my_off;
       float iapp;
@@ -881,15 +1078,33 @@ __global__ void __launch_bounds__(BLOCK, 1) gather_kernel(const __grid_constant_
 }
 
 template <int BLOCK, bool K, bool G>
-cudaError_t launch_gather(const StepArgs& a, int grid, cudaStream_t stream) {
+cudaError_t launch_tgather(const StepArgs& a, int grid, cudaStream_t stream) {
+  const size_t smem = tgather_smem_bytes(a.shape);
+  auto fn = tgather_kernel<BLOCK, K, G>;
+  cudaError_t e = cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+  if (e != cudaSuccess) return e;
   void* args[] = {const_cast<StepArgs*>(&a)};
-  return cudaLaunchCooperativeKernel((const void*)gather_kernel<BLOCK, K, G>, dim3(grid), dim3(BLOCK), args, 0,
-                                     stream);
+  return cudaLaunchCooperativeKernel((const void*)fn, dim3(grid), dim3(BLOCK), args, smem, stream);
+}
+
+template <int BLOCK, bool K, bool G>
+cudaError_t launch_gather(const StepArgs& a, int grid, cudaStream_t stream) {
+  const size_t smem = gather_smem_bytes(BLOCK);
+  auto fn = gather_kernel<BLOCK, K, G>;
+  cudaError_t e = cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+  if (e != cudaSuccess) return e;
+  void* args[] = {const_cast<StepArgs*>(&a)};
+  return cudaLaunchCooperativeKernel((const void*)fn, dim3(grid), dim3(BLOCK), args, smem, stream);
 }
 
 template <int BLOCK>
 cudaError_t launch_gather_block(const StepArgs& a, int grid, cudaStream_t stream) {
   const bool g = a.edge_g != nullptr;
+  if (a.shape.gather == 2) {
+    if (a.shape.kahan) return g ? launch_tgather<BLOCK, true, true>(a, grid, stream)
+                                : launch_tgather<BLOCK, true, false>(a, grid, stream);
+    return g ? launch_tgather<BLOCK, false, true>(a, grid, stream) : launch_tgather<BLOCK, false, false>(a, grid, stream);
+  }
   if (a.shape.kahan) return g ? launch_gather<BLOCK, true, true>(a, grid, stream)
                               : launch_gather<BLOCK, true, false>(a, grid, stream);
   return g ? launch_gather<BLOCK, false, true>(a, grid, stream) : launch_gather<BLOCK, false, false>(a, grid, stream);

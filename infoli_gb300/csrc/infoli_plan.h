@@ -100,10 +100,20 @@ typedef struct {
   int dup_words;   // stamped: second copy of the window starts this many floats in
                    // (a multiple of 32 plus 16, so each word sits in two banks 16
                    // apart); 0 = single copy
-  int gather;      // gather plan: one thread per receiver reads its senders' V_dend
+  int gather;      // 1: gather plan, one thread per receiver reads its senders' V_dend
                    // through L2; edges column by column per CTA (CtaWork::slot_begin
-                   // = first entry, pad0 = padded row length); no dynamic shared memory
+                   // = first entry, pad0 = padded row length); no dynamic shared memory.
+                   // 2: tiled gather plan, V_dend staged tile by tile in shared memory
+                   // (nbuf x tile_cap floats, then 2 mbarriers), one thread per
+                   // receiver; per tile, entries column by column (16-bit offsets from
+                   // the tile start; TileDesc::chunk_begin = first entry, chunk_end =
+                   // padded row length) and per-receiver counts at CtaWork::slot_begin
+                   // + tile * n_cells + receiver
 } SmemShape;
+
+static inline INFOLI_HD size_t tgather_smem_bytes(SmemShape s) {
+  return (((size_t)s.nbuf * (size_t)s.tile_cap * sizeof(float) + 15) & ~(size_t)15) + 2 * sizeof(uint64_t);
+}
 
 // Number of per-cell float arrays kept in shared memory: V_dend, V_soma,
 // V_axon and the nine gate-unit currents.

@@ -331,6 +331,159 @@ static bool make_gather_plan(const PlanInput& in, Plan* out, std::string* err) {
   return true;
 }
 
+// Tiled gather plan: like the gather plan, one thread per receiver, but the
+// senders' V_dend are staged tile by tile into shared memory by bulk copies;
+// per tile, a receiver's senders in that tile (ascending) are stored column by
+// column as 16-bit tile offsets, with per-receiver counts.
+static bool make_tgather_plan(const PlanInput& in, Plan* out, std::string* err) {
+  const int n = in.n, threads = in.threads;
+  const int n_pad = pad_cells(n);
+  int grid = in.grid > 0 ? in.grid : in.grid_max;
+  grid = std::min(grid, in.grid_max);
+  grid = std::max(grid, (n + threads - 1) / threads);
+  if (grid > in.grid_max) {
+    *err = "make_plan: network larger than the co-resident thread count";
+    return false;
+  }
+  std::vector<int> starts = partition_cells(n, in.row_ptr, grid, threads);
+  const int ctas = (int)starts.size() - 1;
+  // per-CTA unique senders and window
+  std::vector<std::vector<int>> uniq(ctas);
+  int max_window = 4;
+#pragma omp parallel for schedule(dynamic, 1) reduction(max : max_window)
+  for (int b = 0; b < ctas; ++b) {
+    std::vector<int>& u = uniq[b];
+    for (int c = starts[b]; c < starts[b + 1]; ++c)
+      for (int64_t e = in.row_ptr[c]; e < in.row_ptr[c + 1]; ++e) u.push_back(in.col[e]);
+    std::sort(u.begin(), u.end());
+    u.erase(std::unique(u.begin(), u.end()), u.end());
+    if (!u.empty()) max_window = std::max(max_window, ((u.back() + 4) & ~3) - (u.front() & ~3));
+  }
+  SmemShape sh{};
+  sh.threads = threads;
+  sh.kahan = in.kahan;
+  sh.edge_g = in.g != nullptr;
+  sh.gather = 2;
+  // one buffer when a CTA's window fits; else two half-size buffers, so the
+  // next tile's copy overlaps this tile's gathers
+  const size_t avail = in.smem_budget > 64 ? in.smem_budget - 64 : 0;
+  const int cap1 = (int)std::min<size_t>(65536, avail / sizeof(float)) & ~3;
+  if (cap1 < 256) {
+    *err = "make_plan: shared memory budget too small";
+    return false;
+  }
+  if (((max_window + 3) & ~3) <= cap1) {
+    sh.nbuf = 1;
+    sh.tile_cap = (max_window + 3) & ~3;
+  } else {
+    sh.nbuf = 2;
+    sh.tile_cap = std::min(65536, (int)(avail / (2 * sizeof(float)))) & ~3;
+  }
+  std::vector<std::vector<TileSpan>> tiles(ctas);
+#pragma omp parallel for schedule(dynamic, 1)
+  for (int b = 0; b < ctas; ++b) tiles[b] = make_tiles(uniq[b], sh.tile_cap, n_pad);
+  // per CTA local tables, then concatenation
+  struct Local {
+    std::vector<TileDesc> tiles;
+    std::vector<uint16_t> edges;
+    std::vector<float> edge_g;
+    std::vector<int32_t> counts;
+  };
+  std::vector<Local> loc(ctas);
+  int cells_cap = 32;
+  for (int b = 0; b < ctas; ++b) cells_cap = std::max(cells_cap, ((starts[b + 1] - starts[b] + 31) / 32) * 32);
+#pragma omp parallel for schedule(dynamic, 1)
+  for (int b = 0; b < ctas; ++b) {
+    Local& L = loc[b];
+    const int nc = starts[b + 1] - starts[b];
+    const std::vector<TileSpan>& tl = tiles[b];
+    // sorted senders per receiver (stable: equal ids keep their order)
+    std::vector<std::vector<std::pair<int, float>>> rows(nc);
+    for (int t = 0; t < nc; ++t) {
+      const int c = starts[b] + t;
+      for (int64_t e = in.row_ptr[c]; e < in.row_ptr[c + 1]; ++e) rows[t].push_back({in.col[e], in.g ? in.g[e] : 0.0f});
+      std::stable_sort(rows[t].begin(), rows[t].end(),
+                       [](const std::pair<int, float>& x, const std::pair<int, float>& y) { return x.first < y.first; });
+    }
+    std::vector<size_t> pos(nc, 0);
+    L.counts.assign((size_t)tl.size() * nc, 0);
+    for (int j = 0; j < (int)tl.size(); ++j) {
+      // this tile's range of each row
+      std::vector<size_t> end(nc);
+      int deg = 0;
+      for (int t = 0; t < nc; ++t) {
+        size_t k = pos[t];
+        while (k < rows[t].size() && rows[t][k].first < tl[j].hi) ++k;
+        end[t] = k;
+        L.counts[(size_t)j * nc + t] = (int32_t)(k - pos[t]);
+        deg = std::max<int>(deg, (int)(k - pos[t]));
+      }
+      TileDesc td{};
+      td.lo = tl[j].lo;
+      td.nfloats = tl[j].hi - tl[j].lo;
+      td.chunk_begin = (int)L.edges.size();  // local; made absolute below
+      td.chunk_end = deg;
+      L.edges.resize(L.edges.size() + (size_t)deg * nc, 0);
+      if (in.g) L.edge_g.resize(L.edge_g.size() + (size_t)deg * nc, 0.0f);
+      for (int t = 0; t < nc; ++t)
+        for (size_t k = pos[t]; k < end[t]; ++k) {
+          const size_t at = (size_t)td.chunk_begin + (k - pos[t]) * nc + t;
+          L.edges[at] = (uint16_t)(rows[t][k].first - td.lo);
+          if (in.g) L.edge_g[at] = rows[t][k].second;
+        }
+      for (int t = 0; t < nc; ++t) pos[t] = end[t];
+      L.tiles.push_back(td);
+    }
+  }
+  Plan& P = *out;
+  P = Plan();
+  P.grid = ctas;
+  P.threads = threads;
+  P.tile_cap = sh.tile_cap;
+  P.nbuf = sh.nbuf;
+  P.cell_slots.assign(n, CellSlots{0, 0});
+  int64_t total_e = 0, total_c = 0;
+  for (int b = 0; b < ctas; ++b) {
+    total_e += (int64_t)loc[b].edges.size();
+    total_c += (int64_t)loc[b].counts.size();
+  }
+  if (total_e > INT32_MAX || total_c > INT32_MAX) {
+    *err = "make_plan: tiled gather plan needs more than 2^31-1 entries";
+    return false;
+  }
+  P.edges.reserve((size_t)total_e);
+  if (in.g) P.edge_g.reserve((size_t)total_e);
+  P.gcol.reserve((size_t)total_c);
+  for (int b = 0; b < ctas; ++b) {
+    Local& L = loc[b];
+    CtaWork w{};
+    w.cell_begin = starts[b];
+    w.n_cells = starts[b + 1] - starts[b];
+    w.tile_begin = (int)P.tiles.size();
+    w.n_tiles = (int)L.tiles.size();
+    w.slot_begin = (int)P.gcol.size();
+    const int e0 = (int)P.edges.size();
+    for (TileDesc td : L.tiles) {
+      td.chunk_begin += e0;
+      P.tiles.push_back(td);
+    }
+    P.edges.insert(P.edges.end(), L.edges.begin(), L.edges.end());
+    if (in.g) P.edge_g.insert(P.edge_g.end(), L.edge_g.begin(), L.edge_g.end());
+    P.gcol.insert(P.gcol.end(), L.counts.begin(), L.counts.end());
+    P.cta.push_back(w);
+    Local().edges.swap(L.edges);
+  }
+  sh.cells_cap = cells_cap;
+  sh.res_tiles = 0;
+  P.shape = sh;
+  P.smem_bytes = tgather_smem_bytes(sh);
+  if (P.smem_bytes > in.smem_budget) {
+    *err = "make_plan: could not fit shared memory";
+    return false;
+  }
+  return true;
+}
+
 bool make_plan(const PlanInput& in, Plan* out, std::string* err) {
   const int n = in.n;
   if (n <= 0 || !in.row_ptr || in.threads <= 0 || in.threads % 32 || in.grid_max <= 0) {
@@ -359,6 +512,7 @@ bool make_plan(const PlanInput& in, Plan* out, std::string* err) {
     return false;
   }
   if (in.sync_mode == kSyncGather) return make_gather_plan(in, out, err);
+  if (in.sync_mode == kSyncTiledGather) return make_tgather_plan(in, out, err);
   const int threads = in.threads;
   const int nwarps = threads / 32;
   const int n_pad = pad_cells(n);
@@ -667,7 +821,7 @@ bool make_plan(const PlanInput& in, Plan* out, std::string* err) {
   // windows larger than shared memory and short rows: gather through L2
   // instead of staging tiles (each row would be cut into a few edges per tile)
   if (!sh.stamped && in.sync_mode == kSyncAuto && E <= (int64_t)kGatherMaxMeanDegree * n)
-    return make_gather_plan(in, out, err);
+    return make_tgather_plan(in, out, err);
   return true;
 }
 
@@ -698,12 +852,39 @@ extern "C" int infoli_plan_emulate(int n, const int64_t* row_ptr, const int32_t*
   std::string err;
   if (!make_plan(in, &P, &err)) return -1;
   const SmemLayout L = smem_layout(P.shape);
-  if (L.total > (size_t)smem_budget) return -2;
+  if (P.shape.gather == 2 ? tgather_smem_bytes(P.shape) > (size_t)smem_budget
+                          : !P.shape.gather && L.total > (size_t)smem_budget)
+    return -2;
   auto fexp = [](float V) { return 0.8f * std::exp(-(V * V) / 100.0f) + 0.2f; };
-  std::vector<unsigned char> sm(L.total);
+  std::vector<unsigned char> sm(P.shape.gather ? 0 : L.total);
   int64_t groups = 0, probes = 0, gather_waves = 0, gathers = 0;
   for (const CtaWork& w : P.cta) {
     if (w.n_cells > threads || w.n_cells > P.shape.cells_cap) return -3;
+    if (P.shape.gather == 2) {
+      if (P.smem_bytes < tgather_smem_bytes(P.shape)) return -2;
+      for (int t = 0; t < w.n_cells; ++t) {
+        const int c = w.cell_begin + t;
+        float acc = 0.0f;
+        for (int j = 0; j < w.n_tiles; ++j) {
+          const TileDesc& td = P.tiles[w.tile_begin + j];
+          if (td.lo < 0 || td.lo % 4 || td.nfloats % 4 || td.nfloats > P.shape.tile_cap) return -4;
+          const size_t ci = (size_t)w.slot_begin + (size_t)j * w.n_cells + t;
+          if (ci >= P.gcol.size()) return -8;
+          const int cnt = P.gcol[ci];
+          if (cnt < 0 || cnt > td.chunk_end) return -8;
+          for (int k = 0; k < cnt; ++k) {
+            const size_t at = (size_t)td.chunk_begin + (size_t)k * w.n_cells + t;
+            if (at >= P.edges.size()) return -8;
+            const int o = P.edges[at];
+            if (o >= td.nfloats || td.lo + o >= n) return -7;
+            const float V = vdend[c] - vdend[td.lo + o];
+            acc += (g ? P.edge_g[at] : 1.0f) * fexp(V) * V;
+          }
+        }
+        ic_out[c] = g ? acc : acc * g_uniform;
+      }
+      continue;
+    }
     if (P.shape.gather) {
       for (int t = 0; t < w.n_cells; ++t) {
         const int c = w.cell_begin + t;
@@ -805,7 +986,7 @@ extern "C" int infoli_plan_emulate(int n, const int64_t* row_ptr, const int32_t*
   }
   if (info) {
     info[0] = P.grid;
-    info[1] = P.shape.gather ? 2 : P.shape.stamped;
+    info[1] = P.shape.gather ? 1 + P.shape.gather : P.shape.stamped;
     info[2] = (int64_t)P.tiles.size();
     info[3] = P.shape.stamped ? groups : (int64_t)P.chunks.size();
     info[4] = P.shape.max_slots;

@@ -37,10 +37,10 @@ struct PlanInput {
   int sync_mode = 0;               // kSyncAuto / kSyncBarrier / kSyncStamped
 };
 
-enum { kSyncAuto = 0, kSyncBarrier = 1, kSyncStamped = 2, kSyncGather = 3 };
+enum { kSyncAuto = 0, kSyncBarrier = 1, kSyncStamped = 2, kSyncGather = 3, kSyncTiledGather = 4 };
 
-// Auto mode picks a gather plan over a barrier plan when the mean degree is
-// at most this (rows too short to fill a warp per chunk once split by tiles).
+// Auto mode picks a tiled gather plan over a barrier plan when the mean degree
+// is at most this (rows too short to fill a warp per chunk once split by tiles).
 enum { kGatherMaxMeanDegree = 384 };
 
 struct Plan {
@@ -55,7 +55,8 @@ struct Plan {
   std::vector<float> edge_g;          // empty unless per-edge g
   std::vector<int> probes;            // stamped mode: progress-probe cells
   std::vector<int2_t> gdesc;          // stamped mode: {slot, recv} per lane-chunk, 32 per group
-  std::vector<int32_t> gcol;          // gather mode: sender ids, column by column per CTA
+  std::vector<int32_t> gcol;          // gather mode: sender ids, column by column per CTA;
+                                      // tiled gather: entries per (tile, receiver)
 };
 
 // Shared-memory bytes the step kernel needs for a plan's parameters.

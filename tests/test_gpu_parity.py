@@ -103,7 +103,7 @@ def test_grid_gaussian_multi_cta(ig, conf):
     assert np.max(np.abs(gpu["soma"] - ref["soma"])) <= TOL_VSOMA_MV
 
 
-@pytest.mark.parametrize("kahan,mode", [(False, "auto"), (True, "auto"), (True, "gather")])
+@pytest.mark.parametrize("kahan,mode", [(False, "auto"), (True, "auto"), (True, "gather"), (True, "tgather")])
 def test_per_edge_g_and_cell_pulses_spike_times(ig, conf, kahan, mode, monkeypatch):
     """CSR with per-edge g ~ U(0.02,0.06), per-cell 5 ms pulses: V_soma over the
     first 2000 steps (before any pulse) and soma spike steps over 1 s.  Onsets are
@@ -126,10 +126,11 @@ def test_per_edge_g_and_cell_pulses_spike_times(ig, conf, kahan, mode, monkeypat
     assert spikes_match(sg, sr)
 
 
-@pytest.mark.parametrize("mode", ["barrier", "gather"])
+@pytest.mark.parametrize("mode", ["barrier", "gather", "tgather"])
 def test_large_window_paths(ig, conf, mode, monkeypatch):
     """A sender window larger than shared memory: several staged tiles per CTA
-    (barrier) or senders read through L2 (gather, the default for short rows)."""
+    (barrier), senders read through L2 (gather), or staged tiles gathered by one
+    thread per receiver (tgather, the default for short rows)."""
     monkeypatch.setenv("INFOLI_SYNC", mode)
     n, k = 90000, 6
     rp, col, g = ig.gen_fixed_degree(n, k, 12, (0.02, 0.06))
@@ -143,7 +144,7 @@ def test_large_window_paths(ig, conf, mode, monkeypatch):
     assert np.max(np.abs(gpu["soma"] - ref["soma"])) <= TOL_VSOMA_MV
 
 
-@pytest.mark.parametrize("mode", ["barrier", "stamped", "gather"])
+@pytest.mark.parametrize("mode", ["barrier", "stamped", "gather", "tgather"])
 def test_exchange_modes_match_oracle(ig, conf, mode, monkeypatch):
     """Every V_dend exchange (grid barrier + bulk tiles; stamped words; grid
     barrier + L2 gathers) on a multi-CTA grid network; each is deterministic

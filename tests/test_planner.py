@@ -73,25 +73,37 @@ def test_per_edge_g_stamped_and_barrier(capi):
 def test_large_window_sparse_rows_gather_else_barrier_tiles(capi):
     rp, col, g = capi.gen_fixed_degree(90000, 6, 12, (0.02, 0.06))
     info = check(capi, 90000, rp, col, g=g)
-    assert info["stamped"] == 2  # auto: short rows over a large window read V_dend through L2
+    assert info["stamped"] == 3  # auto: short rows over a large window: tiled gather
     info = check(capi, 90000, rp, col, g=g, sync_mode=1)
     assert info["stamped"] == 0 and info["tiles"] > info["ctas"]
 
 
-def test_gather_plans(capi):
+@pytest.mark.parametrize("mode,code", [(3, 2), (4, 3)])
+def test_gather_plans(capi, mode, code):
     # ragged rows (uniform generator), per-edge g, empty rows, several grids
     rp, col = capi.gen_uniform(3000, 0.02, 5)
     for grid in (1, 5, 152):
-        info = check(capi, 3000, rp, col, sync_mode=3, grid=grid)
-        assert info["stamped"] == 2 and info["smem_bytes"] == 0
+        info = check(capi, 3000, rp, col, sync_mode=mode, grid=grid)
+        assert info["stamped"] == code and (mode == 4 or info["smem_bytes"] == 0)
     rp, col, g = capi.gen_fixed_degree(4000, 25, 6, (0.02, 0.06))
-    check(capi, 4000, rp, col, g=g, sync_mode=3)
+    check(capi, 4000, rp, col, g=g, sync_mode=mode)
     n = 500
     rp, col = capi.gen_uniform(n, 0.05, 7)
     keep = np.ones(col.size, bool)
     keep[: rp[200]] = False
     rp2 = np.concatenate([[0] * 201, rp[201:] - rp[200]]).astype(np.int64)
-    check(capi, n, rp2, col[keep], sync_mode=3)
+    check(capi, n, rp2, col[keep], sync_mode=mode)
+
+
+def test_tiled_gather_many_tiles_and_small_budget(capi):
+    # a window of 90,000 floats: two buffers and several tiles per CTA; then a
+    # small budget forcing many small tiles
+    rp, col, g = capi.gen_fixed_degree(90000, 6, 12, (0.02, 0.06))
+    info = check(capi, 90000, rp, col, g=g, sync_mode=4)
+    assert info["tiles"] > 2 * info["ctas"]
+    rp, col = capi.gen_uniform(2000, 0.05, 8)
+    info = check(capi, 2000, rp, col, sync_mode=4, smem_budget=4096)
+    assert info["tiles"] > info["ctas"]
 
 
 def test_isolated_cells_and_empty_rows(capi):
