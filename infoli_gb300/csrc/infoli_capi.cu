@@ -217,6 +217,9 @@ int fill_args(infoli_sim* s, StepArgs* a) {
   a->bar = s->d_bar;
   a->err = s->d_err;
   a->timeout_ns = wait_timeout_ns();
+  // failure-detection test hook (see StepArgs::stall_cta); unset in normal use
+  const char* stall = getenv("INFOLI_STALL_CTA");
+  a->stall_cta = stall ? atoi(stall) : -1;
   a->shape = s->plan.shape;
   a->prof = s->d_prof;
   a->vll[0] = s->d_vll[0];

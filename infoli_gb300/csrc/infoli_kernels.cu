@@ -56,7 +56,7 @@ __device__ __forceinline__ bool grid_sync(const StepArgs& a, unsigned target, vo
   if (threadIdx.x == 0) {
     if (t_arrive) *t_arrive = clock64();
     __threadfence();
-    red_release_gpu_add(a.bar, 1u);
+    if ((int)blockIdx.x != a.stall_cta) red_release_gpu_add(a.bar, 1u);
     if (ld_acquire_gpu(a.bar) < target) {
       const uint64_t t0 = globaltimer_ns();
       while (ld_acquire_gpu(a.bar) < target) {
@@ -512,7 +512,8 @@ __global__ void __launch_bounds__(BLOCK, 1) step_kernel(const __grid_constant__ 
   unsigned bar_target = 0;
   if (LL && owner) {
     // publish V^step0 with its stamp (the host cleared both slots before launch)
-    st_relaxed_gpu_u64(a.vll[a.step0 & 1] + cell, pack_stamp(sVd[tid], (unsigned)a.step0));
+    if ((int)blockIdx.x != a.stall_cta)
+      st_relaxed_gpu_u64(a.vll[a.step0 & 1] + cell, pack_stamp(sVd[tid], (unsigned)a.step0));
   }
   for (int t = 0; t < a.n_steps; ++t) {
     const int step = a.step0 + t;
@@ -651,10 +652,10 @@ __global__ void __launch_bounds__(BLOCK, 1) step_kernel(const __grid_constant__ 
       v.Vs = sVs[tid];
       v.Va = sVa[tid];
       voltage_step(a.P, vk, v, cur, ic, iapp);
-      if (LL)
-        st_relaxed_gpu_u64(a.vll[(step + 1) & 1] + cell, pack_stamp(v.Vd, (unsigned)(step + 1)));
-      else
+      if (!LL)
         a.vd[(step + 1) & 1][cell] = v.Vd;
+      else if ((int)blockIdx.x != a.stall_cta)
+        st_relaxed_gpu_u64(a.vll[(step + 1) & 1] + cell, pack_stamp(v.Vd, (unsigned)(step + 1)));
       sVd[tid] = v.Vd;
       sVs[tid] = v.Vs;
       sVa[tid] = v.Va;

@@ -68,6 +68,9 @@ struct StepArgs {
   unsigned* bar;              // grid barrier counter (zeroed before launch)
   int* err;                   // device error word
   unsigned long long timeout_ns;
+  int stall_cta;              // failure-detection test hook: this CTA never arrives at grid
+                              // barriers and never publishes stamped words (-1: none), so
+                              // the other CTAs' bounded waits run out and report an error
   // shared-memory layout (threads = launch block size)
   SmemShape shape;
   // optional per-CTA phase timers (ns, accumulated): [grid][kProfSlots]
