@@ -92,6 +92,11 @@ class ClockSampler:
                                          stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
             self.thread = threading.Thread(target=self._read, daemon=True)
             self.thread.start()
+            # nvidia-smi's own start-up touches the GPU: let it finish before
+            # the timed region (first sample, or 3 s at most)
+            t0 = time.time()
+            while not self.rows and time.time() - t0 < 3.0:
+                time.sleep(0.02)
         except Exception:
             self.proc = None
         return self

@@ -65,7 +65,10 @@ __device__ __forceinline__ void unit_q(const ModelParams& P, const Volts& v, Gat
 __device__ __forceinline__ void unit_rs(const ModelParams& P, const Volts& v, Gates& g, Currents& c) {
   const float Vd = v.Vd;
   const float alpha_r = 1.7f / (1.0f + expf(-(Vd - 5.0f) / 13.9f));
-  const float beta_r = 0.02f * (Vd + 8.5f) / (expf((Vd + 8.5f) / 5.0f) - 1.0f);
+  // removable singularity at Vd = -8.5 (0/0 in the reference's arithmetic):
+  // the limit 0.02 * 5 is used there
+  const float xr = Vd + 8.5f;
+  const float beta_r = xr == 0.0f ? 0.1f : 0.02f * xr / (expf(xr / 5.0f) - 1.0f);
   const float r_inf = alpha_r / (alpha_r + beta_r);
   const float tau_r = 5.0f / (alpha_r + beta_r);
   g.r = P.DELTA * ((r_inf - g.r) / tau_r) + g.r;
@@ -117,7 +120,9 @@ __device__ __forceinline__ void unit_np(const ModelParams& P, const Volts& v, Ga
 // unit 5: voltage-dependent K gate x_s (literal 0.05 step, :632)
 __device__ __forceinline__ void unit_xs(const ModelParams& P, const Volts& v, Gates& g, Currents& c) {
   const float Vs = v.Vs;
-  const float alpha_x_s = 0.13f * (Vs + 25.0f) / (1.0f - expf(-(Vs + 25.0f) / 10.0f));
+  // removable singularity at Vs = -25: the limit 0.13 * 10 is used there
+  const float xs = Vs + 25.0f;
+  const float alpha_x_s = xs == 0.0f ? 1.3f : 0.13f * xs / (1.0f - expf(-xs / 10.0f));
   const float beta_x_s = 1.69f * expf(-0.0125f * (Vs + 35.0f));
   const float x_inf_s = alpha_x_s / (alpha_x_s + beta_x_s);
   const float tau_x_s = 1.0f / (alpha_x_s + beta_x_s);
@@ -139,7 +144,9 @@ __device__ __forceinline__ void unit_mha(const ModelParams& P, const Volts& v, G
 // unit 7: K gate x_a (literal 0.05 step, :661)
 __device__ __forceinline__ void unit_xa(const ModelParams& P, const Volts& v, Gates& g, Currents& c) {
   const float Va = v.Va;
-  const float alpha_x_a = 0.13f * (Va + 25.0f) / (1.0f - expf(-(Va + 25.0f) / 10.0f));
+  // removable singularity at Va = -25: the limit 0.13 * 10 is used there
+  const float xa = Va + 25.0f;
+  const float alpha_x_a = xa == 0.0f ? 1.3f : 0.13f * xa / (1.0f - expf(-xa / 10.0f));
   const float beta_x_a = 1.69f * expf(-0.0125f * (Va + 35.0f));
   const float x_inf_a = alpha_x_a / (alpha_x_a + beta_x_a);
   const float tau_x_a = 1.0f / (alpha_x_a + beta_x_a);

@@ -164,7 +164,11 @@ static inline void cell_f32(const float *P, float **S, int c, float I_c, float i
     float dq_dt = (q_inf - q) / tau_q;
     q = DELTA * dq_dt + q;
     float alpha_r = 1.7f / (1 + expf(-(Vd - 5) / 13.9f));
-    float beta_r = 0.02f * (Vd + 8.5f) / (expf((Vd + 8.5f) / 5) - 1);
+    /* removable singularities (0/0 at Vd = -8.5, Vs = -25, Va = -25 in the
+     * reference's arithmetic, which then turns the whole network to NaN
+     * through the coupling) take their limits; elsewhere the expressions are
+     * the reference's */
+    float beta_r = (Vd + 8.5f) == 0.0f ? 0.1f : 0.02f * (Vd + 8.5f) / (expf((Vd + 8.5f) / 5) - 1);
     float r_inf = alpha_r / (alpha_r + beta_r);
     float tau_r = 5 / (alpha_r + beta_r);
     float dr_dt = (r_inf - r) / tau_r;
@@ -208,7 +212,7 @@ static inline void cell_f32(const float *P, float **S, int c, float I_c, float i
     float dp_dt = (p_inf - pp) / tau_p;
     nn = DELTA * dn_dt + nn;
     pp = DELTA * dp_dt + pp;
-    float alpha_x_s = 0.13f * (Vs + 25) / (1 - expf(-(Vs + 25) / 10));
+    float alpha_x_s = (Vs + 25) == 0.0f ? 1.3f : 0.13f * (Vs + 25) / (1 - expf(-(Vs + 25) / 10));
     float beta_x_s = 1.69f * expf(-0.0125f * (Vs + 35));
     float x_inf_s = alpha_x_s / (alpha_x_s + beta_x_s);
     float tau_x_s = 1 / (alpha_x_s + beta_x_s);
@@ -230,7 +234,7 @@ static inline void cell_f32(const float *P, float **S, int c, float I_c, float i
     float dh_dt_a = (h_inf_a - ha) / tau_h_a;
     float ma = m_inf_a;
     ha = ha + DELTA * dh_dt_a;
-    float alpha_x_a = 0.13f * (Va + 25) / (1 - expf(-(Va + 25) / 10));
+    float alpha_x_a = (Va + 25) == 0.0f ? 1.3f : 0.13f * (Va + 25) / (1 - expf(-(Va + 25) / 10));
     float beta_x_a = 1.69f * expf(-0.0125f * (Va + 35));
     float x_inf_a = alpha_x_a / (alpha_x_a + beta_x_a);
     float tau_x_a = 1 / (alpha_x_a + beta_x_a);
@@ -339,7 +343,7 @@ static inline void cell_f64(const double *P, double **S, int c, double I_c, doub
     double tau_q = 1 / (exp(-0.086 * Vd - 14.6) + exp(0.070 * Vd - 1.87));
     q = DELTA * ((q_inf - q) / tau_q) + q;
     double alpha_r = 1.7 / (1 + exp(-(Vd - 5) / 13.9));
-    double beta_r = 0.02 * (Vd + 8.5) / (exp((Vd + 8.5) / 5) - 1);
+    double beta_r = (Vd + 8.5) == 0.0 ? 0.1 : 0.02 * (Vd + 8.5) / (exp((Vd + 8.5) / 5) - 1);
     double r_inf = alpha_r / (alpha_r + beta_r);
     double tau_r = 5 / (alpha_r + beta_r);
     r = DELTA * ((r_inf - r) / tau_r) + r;
@@ -371,7 +375,7 @@ static inline void cell_f64(const double *P, double **S, int c, double I_c, doub
     double tau_n = 5 + (47 * exp(-(-50 - Vs) / 900));
     nn = DELTA * ((n_inf - nn) / tau_n) + nn;
     pp = DELTA * ((p_inf - pp) / tau_n) + pp;
-    double alpha_x_s = 0.13 * (Vs + 25) / (1 - exp(-(Vs + 25) / 10));
+    double alpha_x_s = (Vs + 25) == 0.0 ? 1.3 : 0.13 * (Vs + 25) / (1 - exp(-(Vs + 25) / 10));
     double beta_x_s = 1.69 * exp(-0.0125 * (Vs + 35));
     double x_inf_s = alpha_x_s / (alpha_x_s + beta_x_s);
     double tau_x_s = 1 / (alpha_x_s + beta_x_s);
@@ -389,7 +393,7 @@ static inline void cell_f64(const double *P, double **S, int c, double I_c, doub
     double h_inf_a = 1 / (1 + exp((-60 - Va) / -5.8));
     double tau_h_a = 1.5 * exp((-40 - Va) / 33);
     ha = ha + DELTA * ((h_inf_a - ha) / tau_h_a);
-    double alpha_x_a = 0.13 * (Va + 25) / (1 - exp(-(Va + 25) / 10));
+    double alpha_x_a = (Va + 25) == 0.0 ? 1.3 : 0.13 * (Va + 25) / (1 - exp(-(Va + 25) / 10));
     double beta_x_a = 1.69 * exp(-0.0125 * (Va + 35));
     double x_inf_a = alpha_x_a / (alpha_x_a + beta_x_a);
     double tau_x_a = 1 / (alpha_x_a + beta_x_a);

@@ -256,3 +256,19 @@ def test_cli_rejects_bad_config(ig, tmp_path):
     exe = os.path.join(os.path.dirname(build.__file__), "_build", "infoli.x")
     r = subprocess.run([exe, "-n", "10", "-c", "bad.conf"], cwd=tmp_path, capture_output=True, text=True)
     assert r.returncode != 0 and "Configuration Error" in r.stdout
+
+
+def test_removable_singularities_stay_finite(ig, conf):
+    """Cells sitting exactly on V_dend = -8.5, V_soma = -25, V_axon = -25 (0/0
+    in the reference's rate expressions) stay finite and match the oracle,
+    which uses the same limits."""
+    n = 64
+    rp, col = ig.gen_uniform(n, 0.3, 2)
+    st0 = hetero_state(conf, n, 1)
+    st0[O.S["V_dend"], ::3] = -8.5
+    st0[O.S["V_soma"], ::2] = -25.0
+    st0[O.S["V_axon"], 1::2] = -25.0
+    # one step (the crafted states are far from equilibrium)
+    gpu, ref, final, st = _compare(ig, conf, n, rp, col, st0, steps=1)
+    assert np.isfinite(final).all() and np.isfinite(st).all()
+    assert np.max(np.abs(final - st)) <= TOL_VSOMA_MV

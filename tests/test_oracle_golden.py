@@ -102,3 +102,29 @@ def test_fp64_twin_close_to_fp32(conf):
     b = O.run(n, conf[:23].astype(np.float64), st64, rp, col, g=g, nsteps=2000, trace_every=1,
               traces=("soma",), fp64=True)["soma"]
     assert np.max(np.abs(a - b)) < 1e-3
+
+
+def test_removable_singularities_take_their_limits():
+    """V_dend = -8.5, V_soma = -25 and V_axon = -25 make three rate
+    expressions 0/0 in the reference's arithmetic (src/openmp/infoli.c:574,
+    :627, :656); one such cell would turn the whole network to NaN through the
+    coupling.  The oracle (and the GPU path) use the limits there."""
+    conf = O.read_parameters(CONF)
+    n = 3
+    st = O.default_state(n, conf)
+    st[O.S["V_dend"]] = [-8.5, -60.0, -8.5]
+    st[O.S["V_soma"]] = [-25.0, -25.0, -60.0]
+    st[O.S["V_axon"]] = [-25.0, -60.0, -25.0]
+    rp = np.array([0, 1, 2, 3], dtype=np.int64)
+    col = np.array([1, 2, 0], dtype=np.int32)
+    # one step: the crafted states are far from equilibrium (later steps
+    # would run away for that reason alone)
+    O.run(n, conf[:23], st, rp, col, g_uniform=0.04, nsteps=1, trace_every=0, traces=())
+    assert np.isfinite(st).all()
+    s64 = O.default_state(n, conf).astype(np.float64)
+    s64[O.S["V_soma"]] = -25.0
+    s64[O.S["V_axon"]] = -25.0
+    s64[O.S["V_dend"]] = -8.5
+    O.run(n, conf[:23].astype(np.float64), s64, rp, col, g_uniform=0.04, nsteps=1, trace_every=0, traces=(),
+          fp64=True)
+    assert np.isfinite(s64).all()
