@@ -8,6 +8,8 @@ Cases (seeded synthetic inputs):
   uniform1k  1,000 cells, the reference generator at p = 0.1
   sparse100k 100,000 cells, 100 senders each, per-edge g U(0.02, 0.06):
            gather plan
+  dense10k 10,000 cells, bitmask generator at p = 0.2 (2,000 senders per
+           cell): stamped plan dominated by the coupling
   batch64  the first 64 networks of the batched workload (sizes log-uniform
            256-8,192, density U(0.05, 0.5)), one graph launch
 Each case builds its inputs, runs K steps once and prints the device time.
@@ -34,6 +36,9 @@ def _sim_case(name, steps):
     elif name == "uniform1k":
         n = 1000
         rp, col = capi.gen_uniform(n, 0.1, 1)
+    elif name == "dense10k":
+        n = 10000
+        rp, col = capi.gen_bitmask_csr(n, 0.2, 5)
     elif name == "sparse100k":
         n = 100000
         rp, col, g = capi.gen_fixed_degree(n, 100, 3, (0.02, 0.06))
@@ -57,7 +62,7 @@ def _batch_case(steps):
 
 def main():
     ap = argparse.ArgumentParser()
-    ap.add_argument("case", choices=["grid10k", "uniform1k", "sparse100k", "batch64"])
+    ap.add_argument("case", choices=["grid10k", "uniform1k", "dense10k", "sparse100k", "batch64"])
     ap.add_argument("--steps", type=int, default=100)
     a = ap.parse_args()
     if a.case == "batch64":

@@ -86,40 +86,6 @@ __device__ __forceinline__ void st_peer(float* local, unsigned peer, float v) {
   asm volatile("st.shared::cluster.f32 [%0], %1;" ::"r"(ra), "f"(v) : "memory");
 }
 
-// Predicated word loads: when `take` is false the destination keeps its value
-// and nothing is read (no branch, so lanes that refill and lanes that do not
-// stay converged).
-__device__ __forceinline__ void ld_shared_if(uint32_t& dst, uint32_t saddr, bool take) {
-  asm volatile("{\n\t.reg .pred p;\n\tsetp.ne.u32 p, %2, 0;\n\t@p ld.shared.u32 %0, [%1];\n\t}"
-               : "+r"(dst)
-               : "r"(saddr), "r"((unsigned)take));
-}
-__device__ __forceinline__ void ld_global_if(uint32_t& dst, const uint32_t* gaddr, bool take) {
-  asm volatile("{\n\t.reg .pred p;\n\tsetp.ne.u32 p, %2, 0;\n\t@p ld.global.nc.u32 %0, [%1];\n\t}"
-               : "+r"(dst)
-               : "l"(gaddr), "r"((unsigned)take));
-}
-__device__ __forceinline__ float ld_shared_f32(uint32_t saddr) {
-  float v;
-  asm volatile("ld.shared.f32 %0, [%1];" : "=f"(v) : "r"(saddr));
-  return v;
-}
-
-template <bool KAHAN>
-__device__ __forceinline__ void add_edge(float& acc, float& cmp, float vc, float vs, bool live) {
-  const float V = vc - vs;
-  const float f = fmaf(0.8f, ex2_approx((V * V) * kNegLog2eOver100), 0.2f);
-  const float term = live ? f * V : 0.0f;
-  if (KAHAN) {
-    const float y = term - cmp;
-    const float s = acc + y;
-    cmp = (s - acc) - y;
-    acc = s;
-  } else {
-    acc += term;
-  }
-}
-
 // Gap-junction currents of a warp's 32 receivers from their bitmask rows,
 // one 32-sender column of the rows at a time.  Words are stored
 // most-significant-bit first (bit 31 of word w = sender 32 w), so a count of

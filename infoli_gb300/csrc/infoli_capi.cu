@@ -326,6 +326,7 @@ int infoli_sim_create(const infoli_sim_desc* d, infoli_sim** out) {
                     : !strcmp(sm, "stamped") ? kSyncStamped
                     : !strcmp(sm, "gather")  ? kSyncGather
                     : !strcmp(sm, "tgather") ? kSyncTiledGather
+                    : !strcmp(sm, "bits")    ? kSyncBits
                                              : kSyncAuto;
   // 512-thread CTAs (128 registers per thread) whenever the network fits in
   // one cell per thread at that size; 1024 threads for larger networks.

@@ -1078,6 +1078,232 @@ __global__ void __launch_bounds__(BLOCK, 1) tgather_kernel(const __grid_constant
   }
 }
 
+// Bitmask plans (one conductance, dense rows, windows larger than shared
+// memory).  Each CTA stages the whole V_dend array tile by tile like the tiled
+// gather kernel; threads are (slice, receiver) pairs, `slices` per receiver,
+// and a warp (32 receivers of one slice) walks its share of each tile's
+// 32-sender columns in lockstep: per column, as many iterations as the fullest
+// of its 32 words has bits, each taking every lane's next set bit (leading
+// zeros) and reading that sender's V_dend inside the same 32 staged floats
+// (no bank conflicts).  Words come from global memory (coalesced: word w of
+// local receiver t at base + w * n_cells + t), two columns ahead.  Column sums
+// are compensated with KAHAN; the slices' sums are added in slice order by the
+// receiver's owner thread, which then runs the cell update.  One grid barrier
+// per step.
+template <bool KAHAN>
+__device__ __forceinline__ void bits_walk(bool own, const uint32_t* gw, int stride, int cs, int ce, uint32_t vtile,
+                                          int c0, float vc, float& acc, float& cmp) {
+  if (cs >= ce) return;
+  uint32_t nx = 0u, nnx = 0u;
+  if (own) {
+    nx = __ldg(gw + (size_t)cs * stride);
+    nnx = __ldg(gw + (size_t)(cs + 1) * stride);
+  }
+  for (int w = cs; w < ce; ++w) {
+    uint32_t x = nx;
+    nx = nnx;
+    ld_global_if(nnx, gw + (size_t)(w + 2) * stride, own);  // rows end with two zero words
+    const int m = (int)__reduce_max_sync(0xffffffffu, (unsigned)__popc(x));
+    const uint32_t vcol = vtile + 128u * (uint32_t)(w - c0);
+    float col = 0.0f;
+    for (int k = 0; k < m; ++k) {
+      const int c = __clz(x);  // 32 once x is used up: reads the next column's first float
+      const bool live = x != 0u;
+      x &= __funnelshift_rc(0x7fffffffu, 0u, (unsigned)c);
+      const float V = vc - ld_shared_f32(vcol + 4u * (uint32_t)c);
+      const float f = fmaf(0.8f, ex2_approx((V * V) * kNegLog2eOver100), 0.2f);
+      if (live) col = fmaf(f, V, col);
+    }
+    if (KAHAN) {
+      const float y = col - cmp;
+      const float t2 = acc + y;
+      cmp = (t2 - acc) - y;
+      acc = t2;
+    } else {
+      acc += col;
+    }
+  }
+}
+
+template <int BLOCK, bool KAHAN>
+__global__ void __launch_bounds__(BLOCK, 1) bits_kernel(const __grid_constant__ StepArgs a) {
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  __shared__ int s_abort;
+  float* tbuf = reinterpret_cast<float*>(smem_raw);
+  const int tile_cap = a.shape.tile_cap, nbuf = a.shape.nbuf;
+  const int R = a.shape.cells_cap, S = a.shape.slices;
+  const size_t toff = ((size_t)nbuf * (size_t)tile_cap * sizeof(float) + 15) & ~(size_t)15;
+  float* part = reinterpret_cast<float*>(smem_raw + toff);  // [S][R] sums, then [S][R] compensations
+  float* partc = part + (size_t)S * R;
+  float* sVd = partc + (size_t)S * R;                       // [R] V_dend of the CTA's receivers
+  uint64_t* mbar = reinterpret_cast<uint64_t*>(reinterpret_cast<unsigned char*>(sVd + R));
+  const CtaWork w = a.cta[blockIdx.x];
+  const TileDesc* tiles = a.tiles + w.tile_begin;
+  const int tid = threadIdx.x;
+  const int slice = tid / R, t = tid % R;
+  const int nc = w.n_cells;
+  const bool owner = slice == 0 && t < nc;
+  const bool walker = slice < S && (t & ~31) < nc;  // warp-uniform
+  const bool own = slice < S && t < nc;
+  const int cell = w.cell_begin + t;
+  const long long np = a.n_pad;
+  if (tid == 0) {
+    mbar_init(&mbar[0], 1);
+    mbar_init(&mbar[1], 1);
+    fence_mbar_init();
+    s_abort = 0;
+  }
+  Volts v{};
+  Gates g{};
+  if (owner) {
+    const float* st = a.st;
+    v.Vd = a.vd[a.step0 & 1][cell];
+    v.Vs = st[F_VS * np + cell];
+    v.Va = st[F_VA * np + cell];
+    g.q = st[F_Q * np + cell];
+    g.r = st[F_R * np + cell];
+    g.s = st[F_S * np + cell];
+    g.Ca = a.ca[cell];
+    g.ICaH = st[F_ICAH * np + cell];
+    g.gCaL = st[F_GCAL * np + cell];
+    g.k = st[F_K * np + cell];
+    g.l = st[F_L * np + cell];
+    g.m = st[F_M * np + cell];
+    g.h = st[F_H * np + cell];
+    g.n = st[F_N * np + cell];
+    g.p = st[F_P * np + cell];
+    g.xs = st[F_XS * np + cell];
+    g.ma = st[F_MA * np + cell];
+    g.ha = st[F_HA * np + cell];
+    g.xa = st[F_XA * np + cell];
+  }
+  float my_amp = 0.0f;
+  int my_onset = 0, my_off = 0;
+  if (owner) {
+    if (a.stim_kind == STIM_CELL) {
+      my_amp = a.cell_amp[cell];
+      my_onset = a.cell_onset[cell];
+    }
+    if (a.cell_step_off) my_off = a.cell_step_off[cell];
+  }
+  const uint32_t* gw = reinterpret_cast<const uint32_t*>(a.gcol) + (size_t)w.slot_begin + (own ? t : 0);
+  const uint32_t tsm = smem_u32(tbuf);
+  const VoltCoef vk = volt_coef(a.P);
+  unsigned bar_target = 0, nload = 0;
+  int row = 0;
+  __syncthreads();
+  for (int st = 0; st < a.n_steps; ++st) {
+    const int step = a.step0 + st;
+    const float* vcur = a.vd[step & 1];
+    if (owner) sVd[t] = v.Vd;
+    if (w.n_tiles > 0 && tid == 0) {
+      fence_proxy_async_global();
+      fence_proxy_async_smem();
+      issue_tile(a, vcur, tiles[0], tbuf + (nload % nbuf) * tile_cap, &mbar[nload % nbuf]);
+    }
+    __syncthreads();
+    const float vc = own ? sVd[t] : 0.0f;
+    float acc = 0.0f, cmp = 0.0f;
+    for (int j = 0; j < w.n_tiles; ++j) {
+      const TileDesc td = tiles[j];
+      const unsigned k = nload + j;
+      const int b = (int)(k % (unsigned)nbuf);
+      if (tid == 0 && j > 0 && nbuf == 1) {
+        fence_proxy_async_smem();
+        issue_tile(a, vcur, td, tbuf, &mbar[0]);
+      }
+      if (tid == 0 && j + 1 < w.n_tiles && nbuf == 2) {
+        fence_proxy_async_smem();
+        const int b1 = (int)((k + 1) & 1u);
+        issue_tile(a, vcur, tiles[j + 1], tbuf + b1 * tile_cap, &mbar[b1]);
+      }
+      if (!wait_tile(a, &mbar[b], (k / (unsigned)nbuf) & 1u)) s_abort = 1;
+      if (walker) {
+        const int c0 = td.chunk_begin, cols = td.chunk_end - td.chunk_begin;
+        const int cs = c0 + (int)((long long)cols * slice / S), ce = c0 + (int)((long long)cols * (slice + 1) / S);
+        bits_walk<KAHAN>(own, gw, nc, cs, ce, tsm + (uint32_t)b * (uint32_t)tile_cap * 4u, c0, vc, acc, cmp);
+      }
+      __syncthreads();  // every thread is done with this buffer before it is refilled
+    }
+    nload += w.n_tiles;
+    if (s_abort) break;
+    if (own) {
+      part[slice * R + t] = acc;
+      partc[slice * R + t] = cmp;
+    }
+    __syncthreads();
+    if (owner) {
+      float sum = 0.0f, c2 = 0.0f;
+      for (int q = 0; q < S; ++q) {
+        if (KAHAN) {
+          const float y = part[q * R + t] - (partc[q * R + t] + c2);
+          const float t2 = sum + y;
+          c2 = (t2 - sum) - y;
+          sum = t2;
+        } else {
+          sum += part[q * R + t];
+        }
+      }
+      const float ic = sum * a.g_uniform;
+      const int ls = step + my_off;
+      float iapp;
+      if (a.stim_kind == STIM_PULSE)
+        iapp = (ls >= a.stim_start && ls < a.stim_end) ? a.stim_amp : 0.0f;
+      else if (a.stim_kind == STIM_CELL)
+        iapp = (ls >= my_onset && ls < my_onset + a.stim_dur) ? my_amp : 0.0f;
+      else
+        iapp = a.stim_table[(size_t)st * np + cell];
+      Currents cur;
+      run_units(a.P, 0xffu, v, g, cur);
+      voltage_step(a.P, vk, v, cur, ic, iapp);
+      a.vd[(step + 1) & 1][cell] = v.Vd;
+      if (a.trace_every > 0 && (step % a.trace_every) == 0) {
+        float* tr = a.trace + (size_t)row * a.trace_nq * np + cell;
+        int qi = 0;
+        if (a.trace_mask & TRACE_AXON) tr[(qi++) * np] = v.Va;
+        if (a.trace_mask & TRACE_SOMA) tr[(qi++) * np] = v.Vs;
+        if (a.trace_mask & TRACE_DEND) tr[(qi++) * np] = v.Vd;
+      }
+    }
+    if (a.trace_every > 0 && (step % a.trace_every) == 0) ++row;
+    if (st + 1 < a.n_steps) {
+      bar_target += gridDim.x;
+      if (!grid_sync(a, bar_target, &s_abort, nullptr)) break;
+    }
+  }
+  if (owner) {
+    float* stp = a.st;
+    stp[F_VS * np + cell] = v.Vs;
+    stp[F_VA * np + cell] = v.Va;
+    stp[F_Q * np + cell] = g.q;
+    stp[F_R * np + cell] = g.r;
+    stp[F_S * np + cell] = g.s;
+    a.ca[cell] = g.Ca;
+    stp[F_ICAH * np + cell] = g.ICaH;
+    stp[F_GCAL * np + cell] = g.gCaL;
+    stp[F_K * np + cell] = g.k;
+    stp[F_L * np + cell] = g.l;
+    stp[F_M * np + cell] = g.m;
+    stp[F_H * np + cell] = g.h;
+    stp[F_N * np + cell] = g.n;
+    stp[F_P * np + cell] = g.p;
+    stp[F_XS * np + cell] = g.xs;
+    stp[F_MA * np + cell] = g.ma;
+    stp[F_HA * np + cell] = g.ha;
+    stp[F_XA * np + cell] = g.xa;
+  }
+}
+
+template <int BLOCK, bool K>
+cudaError_t launch_bits(const StepArgs& a, int grid, cudaStream_t stream) {
+  const size_t smem = tgather_smem_bytes(a.shape);
+  auto fn = bits_kernel<BLOCK, K>;
+  cudaError_t e = cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+  if (e != cudaSuccess) return e;
+  void* args[] = {const_cast<StepArgs*>(&a)};
+  return cudaLaunchCooperativeKernel((const void*)fn, dim3(grid), dim3(BLOCK), args, smem, stream);
+}
+
 template <int BLOCK, bool K, bool G>
 cudaError_t launch_tgather(const StepArgs& a, int grid, cudaStream_t stream) {
   const size_t smem = tgather_smem_bytes(a.shape);
@@ -1101,6 +1327,8 @@ cudaError_t launch_gather(const StepArgs& a, int grid, cudaStream_t stream) {
 template <int BLOCK>
 cudaError_t launch_gather_block(const StepArgs& a, int grid, cudaStream_t stream) {
   const bool g = a.edge_g != nullptr;
+  if (a.shape.gather == 3) return a.shape.kahan ? launch_bits<BLOCK, true>(a, grid, stream)
+                                                 : launch_bits<BLOCK, false>(a, grid, stream);
   if (a.shape.gather == 2) {
     if (a.shape.kahan) return g ? launch_tgather<BLOCK, true, true>(a, grid, stream)
                                 : launch_tgather<BLOCK, true, false>(a, grid, stream);

@@ -108,11 +108,22 @@ typedef struct {
                    // receiver; per tile, entries column by column (16-bit offsets from
                    // the tile start; TileDesc::chunk_begin = first entry, chunk_end =
                    // padded row length) and per-receiver counts at CtaWork::slot_begin
-                   // + tile * n_cells + receiver
+                   // + tile * n_cells + receiver.
+                   // 3: bitmask plan (uniform g), V_dend staged tile by tile as above;
+                   // receivers' adjacency rows as bits (bit 31 of word w = sender 32 w),
+                   // word w of local receiver t at CtaWork::slot_begin + w * n_cells + t,
+                   // two zero words after each row (CtaWork::pad0 = words per row);
+                   // tiles cover whole 32-sender columns (TileDesc::chunk_begin /
+                   // chunk_end = first / end column); `slices` threads share a row
+  int slices;      // bitmask plan: threads per receiver (column slices)
 } SmemShape;
 
 static inline INFOLI_HD size_t tgather_smem_bytes(SmemShape s) {
-  return (((size_t)s.nbuf * (size_t)s.tile_cap * sizeof(float) + 15) & ~(size_t)15) + 2 * sizeof(uint64_t);
+  const size_t tiles = (((size_t)s.nbuf * (size_t)s.tile_cap * sizeof(float) + 15) & ~(size_t)15);
+  // bitmask plans: per-slice partial sums (and compensations) of the receivers
+  const size_t part =
+      s.gather == 3 ? ((size_t)s.slices * 2 + 1) * (size_t)s.cells_cap * sizeof(float) : 0;  // + V_dend
+  return tiles + part + 2 * sizeof(uint64_t);
 }
 
 // Number of per-cell float arrays kept in shared memory: V_dend, V_soma,

@@ -484,6 +484,112 @@ static bool make_tgather_plan(const PlanInput& in, Plan* out, std::string* err) 
   return true;
 }
 
+// Bitmask plan (uniform conductance): cells partitioned over the CTAs; every
+// CTA stages the whole V_dend array tile by tile (tiles of whole 32-sender
+// columns) and its receivers walk their adjacency bits column by column in
+// warp lockstep, `slices` threads per receiver each taking a share of the
+// columns of every tile.
+static bool make_bits_plan(const PlanInput& in, Plan* out, std::string* err) {
+  const int n = in.n, threads = in.threads;
+  if (in.g) {
+    *err = "make_plan: bitmask plans need a uniform conductance";
+    return false;
+  }
+  int grid = in.grid > 0 ? in.grid : in.grid_max;
+  grid = std::min(grid, in.grid_max);
+  grid = std::max(grid, (n + threads - 1) / threads);
+  if (grid > in.grid_max) {
+    *err = "make_plan: network larger than the co-resident thread count";
+    return false;
+  }
+  std::vector<int> starts = partition_cells(n, in.row_ptr, grid, threads);
+  const int ctas = (int)starts.size() - 1;
+  int cells_cap = 32;
+  for (int b = 0; b < ctas; ++b) cells_cap = std::max(cells_cap, ((starts[b + 1] - starts[b] + 31) / 32) * 32);
+  const int wpr = (n + 31) / 32;
+  SmemShape sh{};
+  sh.threads = threads;
+  sh.kahan = in.kahan;
+  sh.edge_g = 0;
+  sh.gather = 3;
+  sh.cells_cap = cells_cap;
+  sh.slices = std::max(1, std::min(8, threads / cells_cap));
+  const size_t part = ((size_t)sh.slices * 2 + 1) * cells_cap * sizeof(float);
+  const size_t avail = in.smem_budget > part + 64 ? in.smem_budget - part - 64 : 0;
+  const int window = wpr * 32;
+  const int cap1 = (int)std::min<size_t>(65536, avail / sizeof(float)) & ~31;
+  if (cap1 < 1024) {
+    *err = "make_plan: shared memory budget too small";
+    return false;
+  }
+  if (window <= cap1) {
+    sh.nbuf = 1;
+    sh.tile_cap = window;
+  } else {
+    sh.nbuf = 2;
+    sh.tile_cap = (int)std::min<size_t>(65536, avail / (2 * sizeof(float))) & ~31;
+  }
+  Plan& P = *out;
+  P = Plan();
+  P.grid = ctas;
+  P.threads = threads;
+  P.tile_cap = sh.tile_cap;
+  P.nbuf = sh.nbuf;
+  P.cell_slots.assign(n, CellSlots{0, 0});
+  int64_t total = 0;
+  for (int b = 0; b < ctas; ++b) total += (int64_t)(starts[b + 1] - starts[b]) * (wpr + 2);
+  if (total > INT32_MAX) {
+    *err = "make_plan: bitmask plan needs more than 2^31-1 words";
+    return false;
+  }
+  P.gcol.assign((size_t)total, 0);
+  // tiles: the same column ranges for every CTA
+  std::vector<TileDesc> tl;
+  const int tcols = sh.tile_cap / 32;
+  for (int c0 = 0; c0 < wpr; c0 += tcols) {
+    TileDesc td{};
+    td.lo = c0 * 32;
+    const int c1 = std::min(wpr, c0 + tcols);
+    td.nfloats = std::min((c1 - c0) * 32, pad_cells(n) - td.lo);
+    td.chunk_begin = c0;
+    td.chunk_end = c1;
+    tl.push_back(td);
+  }
+  int64_t base = 0;
+  for (int b = 0; b < ctas; ++b) {
+    CtaWork w{};
+    w.cell_begin = starts[b];
+    w.n_cells = starts[b + 1] - starts[b];
+    w.tile_begin = (int)P.tiles.size();
+    w.n_tiles = (int)tl.size();
+    w.slot_begin = (int)base;
+    w.pad0 = wpr;
+    P.tiles.insert(P.tiles.end(), tl.begin(), tl.end());
+    P.cta.push_back(w);
+    base += (int64_t)w.n_cells * (wpr + 2);
+  }
+#pragma omp parallel for schedule(dynamic, 1)
+  for (int b = 0; b < ctas; ++b) {
+    const CtaWork& w = P.cta[b];
+    uint32_t* bits = reinterpret_cast<uint32_t*>(P.gcol.data()) + w.slot_begin;
+    for (int t = 0; t < w.n_cells; ++t) {
+      const int c = w.cell_begin + t;
+      for (int64_t e = in.row_ptr[c]; e < in.row_ptr[c + 1]; ++e) {
+        const int s = in.col[e];
+        if (s == c) continue;  // no self-coupling (adds 0 anyway)
+        bits[(size_t)(s >> 5) * w.n_cells + t] |= 0x80000000u >> (s & 31);
+      }
+    }
+  }
+  P.shape = sh;
+  P.smem_bytes = tgather_smem_bytes(sh);
+  if (P.smem_bytes > in.smem_budget) {
+    *err = "make_plan: could not fit shared memory";
+    return false;
+  }
+  return true;
+}
+
 bool make_plan(const PlanInput& in, Plan* out, std::string* err) {
   const int n = in.n;
   if (n <= 0 || !in.row_ptr || in.threads <= 0 || in.threads % 32 || in.grid_max <= 0) {
@@ -513,6 +619,7 @@ bool make_plan(const PlanInput& in, Plan* out, std::string* err) {
   }
   if (in.sync_mode == kSyncGather) return make_gather_plan(in, out, err);
   if (in.sync_mode == kSyncTiledGather) return make_tgather_plan(in, out, err);
+  if (in.sync_mode == kSyncBits) return make_bits_plan(in, out, err);
   const int threads = in.threads;
   const int nwarps = threads / 32;
   const int n_pad = pad_cells(n);
@@ -820,6 +927,11 @@ bool make_plan(const PlanInput& in, Plan* out, std::string* err) {
   P.smem_bytes = smem_layout(sh).total;
   // windows larger than shared memory and short rows: gather through L2
   // instead of staging tiles (each row would be cut into a few edges per tile)
+  // windows larger than shared memory: dense rows with one conductance walk
+  // adjacency bits; short rows gather through staged tiles
+  if (!sh.stamped && in.sync_mode == kSyncAuto && !in.g &&
+      E * kBitsMinDensityInv >= (int64_t)n * (int64_t)n)
+    return make_bits_plan(in, out, err);
   if (!sh.stamped && in.sync_mode == kSyncAuto && E <= (int64_t)kGatherMaxMeanDegree * n)
     return make_tgather_plan(in, out, err);
   return true;
@@ -852,7 +964,7 @@ extern "C" int infoli_plan_emulate(int n, const int64_t* row_ptr, const int32_t*
   std::string err;
   if (!make_plan(in, &P, &err)) return -1;
   const SmemLayout L = smem_layout(P.shape);
-  if (P.shape.gather == 2 ? tgather_smem_bytes(P.shape) > (size_t)smem_budget
+  if (P.shape.gather >= 2 ? tgather_smem_bytes(P.shape) > (size_t)smem_budget
                           : !P.shape.gather && L.total > (size_t)smem_budget)
     return -2;
   auto fexp = [](float V) { return 0.8f * std::exp(-(V * V) / 100.0f) + 0.2f; };
@@ -860,6 +972,31 @@ extern "C" int infoli_plan_emulate(int n, const int64_t* row_ptr, const int32_t*
   int64_t groups = 0, probes = 0, gather_waves = 0, gathers = 0;
   for (const CtaWork& w : P.cta) {
     if (w.n_cells > threads || w.n_cells > P.shape.cells_cap) return -3;
+    if (P.shape.gather == 3) {
+      const int wpr = w.pad0;
+      for (int t = 0; t < w.n_cells; ++t) {
+        const int c = w.cell_begin + t;
+        float acc = 0.0f;
+        for (int j = 0; j < w.n_tiles; ++j) {
+          const TileDesc& td = P.tiles[w.tile_begin + j];
+          if (td.lo != td.chunk_begin * 32 || td.nfloats > P.shape.tile_cap || td.lo % 32) return -4;
+          for (int col = td.chunk_begin; col < td.chunk_end; ++col) {
+            const size_t at = (size_t)w.slot_begin + (size_t)col * w.n_cells + t;
+            if (col >= wpr || at >= P.gcol.size()) return -8;
+            const uint32_t x = (uint32_t)P.gcol[at];
+            for (int k = 0; k < 32; ++k)
+              if (x & (0x80000000u >> k)) {
+                const int s = col * 32 + k;
+                if (s >= n || s - td.lo >= td.nfloats) return -7;
+                const float V = vdend[c] - vdend[s];
+                acc += fexp(V) * V;
+              }
+          }
+        }
+        ic_out[c] = acc * g_uniform;
+      }
+      continue;
+    }
     if (P.shape.gather == 2) {
       if (P.smem_bytes < tgather_smem_bytes(P.shape)) return -2;
       for (int t = 0; t < w.n_cells; ++t) {

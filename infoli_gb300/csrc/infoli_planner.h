@@ -37,7 +37,11 @@ struct PlanInput {
   int sync_mode = 0;               // kSyncAuto / kSyncBarrier / kSyncStamped
 };
 
-enum { kSyncAuto = 0, kSyncBarrier = 1, kSyncStamped = 2, kSyncGather = 3, kSyncTiledGather = 4 };
+enum { kSyncAuto = 0, kSyncBarrier = 1, kSyncStamped = 2, kSyncGather = 3, kSyncTiledGather = 4, kSyncBits = 5 };
+
+// Auto mode picks a bitmask plan (uniform g only) over tile/gather plans when
+// the density is at least 1 / kBitsMinDensityInv.
+enum { kBitsMinDensityInv = 16 };
 
 // Auto mode picks a tiled gather plan over a barrier plan when the mean degree
 // is at most this (rows too short to fill a warp per chunk once split by tiles).
@@ -56,7 +60,8 @@ struct Plan {
   std::vector<int> probes;            // stamped mode: progress-probe cells
   std::vector<int2_t> gdesc;          // stamped mode: {slot, recv} per lane-chunk, 32 per group
   std::vector<int32_t> gcol;          // gather mode: sender ids, column by column per CTA;
-                                      // tiled gather: entries per (tile, receiver)
+                                      // tiled gather: entries per (tile, receiver);
+                                      // bitmask plans: the rows' bit words
 };
 
 // Shared-memory bytes the step kernel needs for a plan's parameters.

@@ -102,4 +102,24 @@ __device__ __forceinline__ void bulk_g2s(void* dst, const void* src, unsigned by
       : "memory");
 }
 
+
+// Predicated word loads: when `take` is false the destination keeps its value
+// and nothing is read (no branch, so lanes that load and lanes that do not
+// stay converged).
+__device__ __forceinline__ void ld_shared_if(uint32_t& dst, uint32_t saddr, bool take) {
+  asm volatile("{\n\t.reg .pred p;\n\tsetp.ne.u32 p, %2, 0;\n\t@p ld.shared.u32 %0, [%1];\n\t}"
+               : "+r"(dst)
+               : "r"(saddr), "r"((unsigned)take));
+}
+__device__ __forceinline__ void ld_global_if(uint32_t& dst, const uint32_t* gaddr, bool take) {
+  asm volatile("{\n\t.reg .pred p;\n\tsetp.ne.u32 p, %2, 0;\n\t@p ld.global.nc.u32 %0, [%1];\n\t}"
+               : "+r"(dst)
+               : "l"(gaddr), "r"((unsigned)take));
+}
+__device__ __forceinline__ float ld_shared_f32(uint32_t saddr) {
+  float v;
+  asm volatile("ld.shared.f32 %0, [%1];" : "=f"(v) : "r"(saddr));
+  return v;
+}
+
 }  // namespace infoli

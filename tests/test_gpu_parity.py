@@ -144,7 +144,7 @@ def test_large_window_paths(ig, conf, mode, monkeypatch):
     assert np.max(np.abs(gpu["soma"] - ref["soma"])) <= TOL_VSOMA_MV
 
 
-@pytest.mark.parametrize("mode", ["barrier", "stamped", "gather", "tgather"])
+@pytest.mark.parametrize("mode", ["barrier", "stamped", "gather", "tgather", "bits"])
 def test_exchange_modes_match_oracle(ig, conf, mode, monkeypatch):
     """Every V_dend exchange (grid barrier + bulk tiles; stamped words; grid
     barrier + L2 gathers) on a multi-CTA grid network; each is deterministic
@@ -272,3 +272,19 @@ def test_removable_singularities_stay_finite(ig, conf):
     gpu, ref, final, st = _compare(ig, conf, n, rp, col, st0, steps=1)
     assert np.isfinite(final).all() and np.isfinite(st).all()
     assert np.max(np.abs(final - st)) <= TOL_VSOMA_MV
+
+
+@pytest.mark.parametrize("kahan", [False, True])
+def test_bitmask_plan_dense_network(ig, conf, kahan, monkeypatch):
+    """Dense random network with one conductance on the bitmask plan (several
+    column slices per receiver, two V_dend tiles): V_soma within tolerance of
+    the oracle, spikes within one step, deterministic."""
+    monkeypatch.setenv("INFOLI_SYNC", "bits")
+    n = 3000
+    rp, col = ig.gen_bitmask_csr(n, 0.2, 5)
+    st0 = hetero_state(conf, n, 4)
+    gpu, ref, _, _ = _compare(ig, conf, n, rp, col, st0, steps=2000, kahan=kahan, nthreads=16)
+    assert np.max(np.abs(gpu["soma"] - ref["soma"])) <= TOL_VSOMA_MV
+    with ig.Simulation(n, conf, rp, col, init_state=st0, kahan=kahan) as a, \
+            ig.Simulation(n, conf, rp, col, init_state=st0, kahan=kahan) as b:
+        assert np.array_equal(a.run(300, 1, 4)["dend"], b.run(300, 1, 4)["dend"])

@@ -122,3 +122,21 @@ def test_stamped_request_that_cannot_fit_is_rejected(capi):
     rp, col, g = capi.gen_fixed_degree(90000, 6, 12, (0.02, 0.06))
     with pytest.raises(capi.InfoliError):
         capi.plan_emulate(90000, rp, col, np.zeros(90000, np.float32), g=g, sync_mode=2)
+
+
+def test_bitmask_plans(capi):
+    """Bitmask plans (uniform g): one tile, several tiles (small budget) and
+    ragged CTAs; the emulation walks the bit rows with the kernel's layout."""
+    rp, col = capi.gen_bitmask_csr(3000, 0.2, 5)
+    for grid in (1, 7, 152):
+        info = check(capi, 3000, rp, col, sync_mode=5, grid=grid)
+        assert info["stamped"] == 4
+    info = check(capi, 3000, rp, col, sync_mode=5, smem_budget=8 * 1024)
+    assert info["tiles"] > info["ctas"]
+    # auto picks it for dense rows over a window larger than shared memory
+    rp, col = capi.gen_bitmask_csr(60000, 0.08, 6)
+    info = check(capi, 60000, rp, col)
+    assert info["stamped"] == 4 and info["tiles"] >= 2 * info["ctas"]
+    with pytest.raises(capi.InfoliError):
+        capi.plan_emulate(100, *capi.gen_fixed_degree(100, 5, 1, (0.02, 0.06))[:2], np.zeros(100, np.float32),
+                          g=np.full(500, 0.04, np.float32), sync_mode=5)
