@@ -351,7 +351,7 @@ typedef struct {
   int device;
   int64_t hbm_budget;    /* device bytes admitted requests may hold; 0 = 80% of free memory */
   int max_active;        /* requests admitted at once (preparing or running); 0 = 16 */
-  int64_t work_per_cta;  /* edge evaluations per step per CTA when sizing a request's SM share; 0 = 262144 */
+  int64_t work_per_cta;  /* edge evaluations per step per CTA when sizing a request's SM share; 0 = 32768 */
   int backfill_ms;       /* later requests may pass a head request that does not fit yet for this long; 0 = 1000 */
   int prep_threads;      /* host threads building plans; 0 = 4 */
   int flags;             /* INFOLI_F_KAHAN for every request */

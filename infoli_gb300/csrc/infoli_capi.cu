@@ -344,6 +344,13 @@ int infoli_sim_create(const infoli_sim_desc* d, infoli_sim** out) {
       break;
     }
   }
+  // plans with one thread per receiver (gather, tiled gather, bitmask) hide
+  // their load latency with more warps: 1024-thread CTAs when the choice is free
+  if (planned && !want_threads && s->plan.shape.gather && s->plan.threads == 512) {
+    Plan wide;
+    pin.threads = kThreads;
+    if (make_plan(pin, &wide, &perr) && wide.shape.gather == s->plan.shape.gather) s->plan = std::move(wide);
+  }
   if (!planned) return fail(infoli__fail(INFOLI_ERR_ARG, "%s", perr.c_str()));
   const int cores = max_coresident_ctas(s->plan.threads, s->plan.smem_bytes);
   if (cores < s->plan.grid)

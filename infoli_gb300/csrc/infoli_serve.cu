@@ -276,7 +276,7 @@ extern "C" int infoli_server_create(const infoli_server_desc* d, infoli_server**
   sv->device = d->device;
   sv->flags = d->flags;
   sv->max_active = d->max_active > 0 ? d->max_active : 16;
-  sv->work_per_cta = d->work_per_cta > 0 ? d->work_per_cta : (int64_t)1 << 18;
+  sv->work_per_cta = d->work_per_cta > 0 ? d->work_per_cta : (int64_t)1 << 15;
   sv->backfill_s = d->backfill_ms > 0 ? d->backfill_ms * 1e-3 : 1.0;
   cudaSetDevice(sv->device);
   cudaDeviceGetAttribute(&sv->nsm, cudaDevAttrMultiProcessorCount, sv->device);
