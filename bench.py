@@ -34,6 +34,7 @@ sys.path.insert(0, ROOT)
 ROWS, COLS, SIGMA, RADIUS, SEED = 100, 100, 10.0, 18.0, 1
 STEPS_PER_ITER = 1000
 TRACE_EVERY = 100
+CPU_SAMPLE_STEPS = 5000  # about 10 s of the port on 16 host cores
 
 
 def ncu_traffic():
@@ -284,7 +285,7 @@ def run_gpu(args, world, rank, local):
     if rank == 0:
         clocks = clk.summary()
         threads = os.cpu_count() or 1
-        cpu_rate, cpu_dt = cpu_port_rate(conf, n, rp, col, st, 200, threads)
+        cpu_rate, cpu_dt = cpu_port_rate(conf, n, rp, col, st, CPU_SAMPLE_STEPS, threads)
         result = {
             "metric": "cell-steps/s", "value": value, "unit": "cell-steps/s", "n_gpus": world,
             "steps": args.steps, "warmup": args.warmup, "ms_per_step": total_dev_ms / args.steps,
@@ -312,7 +313,7 @@ def run_gpu(args, world, rank, local):
             "phase_ns_per_timestep": prof["max"],
             "clocks": clocks,
             "cpu_baseline": {"value": cpu_rate, "unit": "cell-steps/s", "cores": threads, "kind": "port",
-                             "sample": f"200 timesteps of the same workload ({cpu_dt:.1f} s)"},
+                             "sample": f"{CPU_SAMPLE_STEPS} timesteps of the same workload ({cpu_dt:.1f} s)"},
         }
         print(json.dumps(result))
     return 0
