@@ -288,3 +288,33 @@ def test_bitmask_plan_dense_network(ig, conf, kahan, monkeypatch):
     with ig.Simulation(n, conf, rp, col, init_state=st0, kahan=kahan) as a, \
             ig.Simulation(n, conf, rp, col, init_state=st0, kahan=kahan) as b:
         assert np.array_equal(a.run(300, 1, 4)["dend"], b.run(300, 1, 4)["dend"])
+
+
+@pytest.mark.parametrize("mode", ["auto", "barrier", "tgather", "bits"])
+@pytest.mark.parametrize("n", [1, 2, 33])
+def test_tiny_networks(ig, conf, n, mode, monkeypatch):
+    """Edge sizes: a single cell (no edges), two coupled cells, one cell more
+    than a warp; every exchange mode that applies."""
+    monkeypatch.setenv("INFOLI_SYNC", mode if mode != "auto" else "")
+    if n == 1:
+        rp, col = np.array([0, 0], np.int64), np.zeros(0, np.int32)
+    else:
+        rp, col = ig.gen_uniform(n, 0.7, 3)
+    st0 = hetero_state(conf, n, 5)
+    gpu, ref, final, _ = _compare(ig, conf, n, rp, col, st0, steps=300)
+    assert np.isfinite(final).all()
+    assert np.max(np.abs(gpu["soma"] - ref["soma"])) <= TOL_VSOMA_MV
+
+
+def test_batch_with_tiny_networks(ig, conf):
+    nets = [(1, np.zeros((1, 1), np.uint32), 0.04), (2, ig.gen_bitmask(2, 1.0, 1), 0.04),
+            (33, ig.gen_bitmask(33, 0.5, 2), 0.05)]
+    st0 = np.concatenate([hetero_state(conf, n, 9 + i) for i, (n, _, _) in enumerate(nets)], axis=1)
+    with ig.Batch(conf, nets, init_state=st0) as bt:
+        bt.run(300)
+        got = bt.get_state()
+        for i, (n, bits, g) in enumerate(nets):
+            rp, col = ig.bitmask_to_csr(n, bits)
+            s = np.ascontiguousarray(bt.net_state(st0, i)).copy()
+            O.run(n, conf[:23], s, rp, col, g_uniform=g, nsteps=300, trace_every=0, traces=())
+            assert np.max(np.abs(bt.net_state(got, i)[O.S["V_soma"]] - s[O.S["V_soma"]])) <= TOL_VSOMA_MV
