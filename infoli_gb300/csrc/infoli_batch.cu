@@ -416,6 +416,7 @@ cudaError_t launch_group(const infoli_batch* b, const BatchGroup& g, BatchArgs a
 
 extern "C" int infoli_batch_create(const infoli_batch_desc* d, infoli_batch** out) {
   infoli__clear_error();
+  InfoliRange nvtx_range("infoli_batch_create");
   if (!d || !out || d->n_nets <= 0 || !d->n_cells || !d->params || !d->bits || !d->g ||
       (!d->init_state && !d->init_values))
     return infoli__fail(INFOLI_ERR_ARG, "batch_create: bad argument");
@@ -578,6 +579,7 @@ extern "C" int infoli_batch_set_stimulus_pulse(infoli_batch* b, int start_step, 
 
 extern "C" int infoli_batch_run(infoli_batch* b, int n_steps) {
   infoli__clear_error();
+  InfoliRange nvtx_range("infoli_batch_run");
   if (!b || n_steps < 0) return infoli__fail(INFOLI_ERR_ARG, "batch_run: bad argument");
   BK(cudaSetDevice(b->device));
   if (b->graph_steps != n_steps) {

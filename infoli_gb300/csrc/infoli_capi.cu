@@ -274,6 +274,7 @@ int infoli_device_count(void) {
 
 int infoli_sim_create(const infoli_sim_desc* d, infoli_sim** out) {
   infoli__clear_error();
+  InfoliRange nvtx_range("infoli_sim_create");
   if (!d || !out) return infoli__fail(INFOLI_ERR_ARG, "sim_create: null argument");
   *out = nullptr;
   if (d->n_cells <= 0) return infoli__fail(INFOLI_ERR_ARG, "sim_create: n_cells must be positive");
@@ -495,6 +496,7 @@ const float* table_at(const infoli_sim* s, int step0) {
 
 int infoli_sim_run(infoli_sim* s, int n_steps, int trace_every, int trace_what, infoli_trace_cb cb, void* user) {
   infoli__clear_error();
+  InfoliRange nvtx_range("infoli_sim_run");
   if (!s || n_steps < 0) return infoli__fail(INFOLI_ERR_ARG, "sim_run: bad argument");
   if (trace_every > 0 && (!cb || nq_of(trace_what) == 0))
     return infoli__fail(INFOLI_ERR_ARG, "sim_run: tracing needs a callback and at least one quantity");
@@ -607,6 +609,7 @@ int infoli_sim_run(infoli_sim* s, int n_steps, int trace_every, int trace_what, 
 
 int infoli_sim_launch(infoli_sim* s, int n_steps) {
   infoli__clear_error();
+  InfoliRange nvtx_range("infoli_sim_launch");
   if (!s || n_steps < 0) return infoli__fail(INFOLI_ERR_ARG, "sim_launch: bad argument");
   CK(cudaSetDevice(s->device));
   if (int rc0 = check_table_range(s, n_steps)) return rc0;

@@ -16,6 +16,17 @@ void infoli__clear_error(void);
 
 #ifdef __cplusplus
 }
+
+#include <nvtx3/nvToolsExt.h>
+
+/* Named NVTX range for the host phases (plan, upload, run, retire), so a
+ * system profiler's timeline shows them; header-only, no library. */
+struct InfoliRange {
+  explicit InfoliRange(const char* name) { nvtxRangePushA(name); }
+  ~InfoliRange() { nvtxRangePop(); }
+  InfoliRange(const InfoliRange&) = delete;
+  InfoliRange& operator=(const InfoliRange&) = delete;
+};
 #endif
 
 #endif

@@ -129,6 +129,7 @@ void prep_loop(infoli_server* sv) {
     sv->to_prep.pop_front();
     ++sv->preparing;
     lk.unlock();
+    InfoliRange nvtx_range("infoli_server_prepare");
     infoli_sim_desc d;
     std::memset(&d, 0, sizeof d);
     d.n_cells = r->n;
