@@ -10,4 +10,6 @@ import bench  # noqa: E402
 world, rank, local = bench.dist_setup()
 mx = bench.dist_max(10.0 * (rank + 1), world)
 bench.dist_barrier(world)
-print(json.dumps({"rank": rank, "world": world, "local": local, "max": mx}), flush=True)
+# one write per line: the ranks share the launcher's stdout pipe, and a single
+# write of less than PIPE_BUF bytes is not interleaved with the other rank's
+os.write(1, (json.dumps({"rank": rank, "world": world, "local": local, "max": mx}) + "\n").encode())
