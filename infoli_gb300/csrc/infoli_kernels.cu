@@ -137,9 +137,10 @@ __device__ __forceinline__ unsigned long long pack_stamp(float v, unsigned stamp
 }
 
 // Stamped exchange.  A CTA's window is one flat index space: word i <
-// tile_words is word i of its tiles laid end to end (as they sit in shared
-// memory), word i >= tile_words is progress probe i - tile_words (checked,
-// not stored).  Words of cells >= n_cells are never published and read as 0.
+// tile_words is the V_dend of its i-th unique sender (ascending cell ids,
+// held in shared memory; the value lands at float i of the window buffer),
+// word i >= tile_words is progress probe i - tile_words (checked, not
+// stored).  Words of cells >= n_cells are never published and read as 0.
 // Polling thread pt of T takes words pt, pt + T, ... in batches of
 // kPollBatch loads in flight.  A batch can be issued early and finished later
 // (the loads overlap other work); every wait is bounded by the launch's
@@ -147,8 +148,7 @@ __device__ __forceinline__ unsigned long long pack_stamp(float v, unsigned stamp
 constexpr int kPollBatch = 8;
 
 struct PollWindow {
-  const TileDesc* tiles;
-  int n_tiles;
+  const int* cells;  // the window's sender ids (shared memory)
   const int* probes;
   int n_probes;
   int tile_words;
@@ -167,17 +167,8 @@ __device__ __forceinline__ int window_cell(const PollWindow& pw, int i, int* dst
     *dst = -1;
     return pw.probes[i - pw.tile_words];
   }
-  int toff = 0;
-  for (int j = 0; j < pw.n_tiles; ++j) {
-    const int nf = pw.tiles[j].nfloats;
-    if (i < toff + nf) {
-      *dst = i;
-      return pw.tiles[j].lo + (i - toff);
-    }
-    toff += nf;
-  }
-  *dst = -1;
-  return 0;
+  *dst = i;
+  return pw.cells[i];
 }
 
 // tbuf receives each word at its window index and, when dup > 0, again at
@@ -390,10 +381,9 @@ __global__ void __launch_bounds__(BLOCK, 1) step_kernel(const __grid_constant__ 
   PollWindow pw{};
   int poll_first = 0;
   if (LL) {
-    pw.n_tiles = w.n_tiles;
     pw.probes = a.probes + w.probe_begin;
     pw.n_probes = w.n_probes;
-    for (int j = 0; j < w.n_tiles; ++j) pw.tile_words += a.tiles[w.tile_begin + j].nfloats;
+    pw.tile_words = w.n_tiles;  // stamped plans: window words (gcol[tile_begin ..])
     pw.total = pw.tile_words + pw.n_probes;
     const int pollers = (int)blockDim.x - ngroups * U * 32;
     if (ngroups * U < nwarps && pollers * kPollBatch >= pw.total) poll_first = ngroups * U * 32;
@@ -403,18 +393,19 @@ __global__ void __launch_bounds__(BLOCK, 1) step_kernel(const __grid_constant__ 
 
   // ---- static work: either resident in shared memory or read from global.
   // Indices below are relative to the CTA's first chunk / edge.
-  const TileDesc* tiles = a.tiles + w.tile_begin;
+  const TileDesc* tiles = LL ? nullptr : a.tiles + w.tile_begin;  // stamped: tile_begin indexes gcol
   const ChunkDesc* chunks = a.chunks;
   const uint16_t* edges = a.edges;
   const float* edge_g = a.edge_g;
   int chunk0 = 0, edge0 = 0;
   if (LL) {
-    // stamped plans: tiles + packed lane-chunk groups, copied once per launch
-    TileDesc* s_t = reinterpret_cast<TileDesc*>(smem_raw + L.tdesc);
+    // stamped plans: window sender ids (in the descriptor area) + packed
+    // lane-chunk groups, copied once per launch
+    int* s_w = reinterpret_cast<int*>(smem_raw + L.tdesc);
     int2* s_d = reinterpret_cast<int2*>(smem_raw + L.chunks);
     uint2* s_e = reinterpret_cast<uint2*>(smem_raw + L.edges);
     float4* s_g = reinterpret_cast<float4*>(smem_raw + L.eg);
-    for (int i = tid; i < w.n_tiles; i += blockDim.x) s_t[i] = tiles[i];
+    for (int i = tid; i < w.n_tiles; i += blockDim.x) s_w[i] = a.gcol[w.tile_begin + i];
     const int nd = w.n_groups * 32;
     for (int i = tid; i < nd; i += blockDim.x) s_d[i] = a.gdesc[(size_t)w.group_begin * 32 + i];
     const int nq = w.n_groups * (kGroupEntries / 4);  // 8-byte quads
@@ -424,8 +415,7 @@ __global__ void __launch_bounds__(BLOCK, 1) step_kernel(const __grid_constant__ 
       const float4* gg = reinterpret_cast<const float4*>(a.edge_g) + (size_t)w.group_begin * (kGroupEntries / 4);
       for (int i = tid; i < nq; i += blockDim.x) s_g[i] = gg[i];
     }
-    tiles = s_t;
-    pw.tiles = s_t;
+    pw.cells = s_w;
   } else if (w.n_tiles > 0) {
     chunk0 = tiles[0].chunk_begin;
     const int chunk1 = tiles[w.n_tiles - 1].chunk_end;

@@ -20,12 +20,15 @@
 // Two ways of exchanging V_dend between steps:
 //   * barrier mode: V_dend double buffer in global memory, one grid barrier
 //     per step, tiles staged by bulk async copies (any window size);
-//   * stamped mode (all of a CTA's tiles fit in shared memory at once): every
+//   * stamped mode (every CTA's window fits in shared memory at once): every
 //     cell publishes (V_dend, step) as one 64-bit word into a two-slot array;
-//     a CTA polls exactly the words it reads (plus one word of every CTA that
-//     reads it without being read by it, so no slot is overwritten before its
-//     readers are done) until their stamps show the step it needs.  No grid
-//     barrier: each CTA waits only for its own neighbourhood.
+//     a CTA polls exactly the words it reads -- its window, the sorted list of
+//     its receivers' unique senders, kept in the plan's gcol table at
+//     CtaWork::tile_begin (n_tiles entries; stamped plans have no tiles) --
+//     plus one word of every CTA that reads it without being read by it, so
+//     no slot is overwritten before its readers are done, until their stamps
+//     show the step it needs.  No grid barrier: each CTA waits only for its
+//     own neighbourhood.
 #pragma once
 #include <stddef.h>
 #include <stdint.h>
@@ -92,11 +95,12 @@ typedef struct {
   int cells_cap;   // owned cells per CTA (max over CTAs, multiple of 32)
   int max_slots;   // partial-sum slots per CTA
   int kahan;       // compensated sums (second slot array)
-  int res_tiles;   // resident tile descriptors per CTA (0: not resident)
+  int res_tiles;   // resident tile descriptors per CTA (0: not resident); stamped
+                   // plans keep the window's sender ids there, four per slot
   int res_chunks;  // resident chunk descriptors per CTA (stamped: lane-chunks, 16 B each)
   int res_edges;   // resident edge offsets per CTA
   int edge_g;      // per-edge conductances present
-  int stamped;     // stamped exchange (all tiles resident at once, nbuf = 1)
+  int stamped;     // stamped exchange (the whole window resident at once, nbuf = 1)
   int dup_words;   // stamped: second copy of the window starts this many floats in
                    // (a multiple of 32 plus 16, so each word sits in two banks 16
                    // apart); 0 = single copy

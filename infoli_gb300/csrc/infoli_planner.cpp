@@ -88,14 +88,15 @@ std::vector<TileSpan> make_tiles(const std::vector<int>& u, int cap, int n_pad) 
 
 // Build the packed lane-chunk tables of a stamped, resident plan (see
 // infoli_plan.h): per receiver, its senders (ascending) become byte offsets
-// into the CTA's concatenated tiles, cut into lane-chunks of kLaneEdges;
+// into the CTA's window (its sorted unique senders, win[b], one float each),
+// cut into lane-chunks of kLaneEdges;
 // the chunks of a CTA, receiver-major, are dealt 32 per group.  Inside a
 // group, entries are permuted per chunk so that the 32 lanes reading
 // position k hit distinct shared-memory banks where possible.  Receiver slots
 // are rewritten to the lane-chunks (receiver-major, so a receiver's partial
 // sums stay contiguous and in sender order); the last group of a CTA is
 // filled with dummy chunks that write one spare slot.
-void pack_groups(Plan& P, const SmemLayout& L, const PlanInput& in, const std::vector<int>& starts,
+void pack_groups(Plan& P, const SmemLayout& L, const PlanInput& in, const std::vector<std::vector<int>>& win,
                  int dup_words) {
   const bool edge_g = in.g != nullptr;
   std::vector<int2_t> gdesc;
@@ -104,16 +105,7 @@ void pack_groups(Plan& P, const SmemLayout& L, const PlanInput& in, const std::v
   int max_slots = 1;
   for (size_t b = 0; b < P.cta.size(); ++b) {
     CtaWork& w = P.cta[b];
-    // tile table of this CTA with offsets into the concatenated buffer
-    std::vector<int> tlo, thi, toff;
-    int off = 0;
-    for (int j = 0; j < w.n_tiles; ++j) {
-      const TileDesc& td = P.tiles[w.tile_begin + j];
-      tlo.push_back(td.lo);
-      thi.push_back(td.lo + td.nfloats);
-      toff.push_back(off);
-      off += td.nfloats;
-    }
+    const std::vector<int>& u = win[b];
     struct LaneChunk {
       int recv, slot;
       std::vector<std::pair<uint16_t, float>> e;
@@ -127,15 +119,15 @@ void pack_groups(Plan& P, const SmemLayout& L, const PlanInput& in, const std::v
       std::stable_sort(snd.begin(), snd.end(),
                        [](const std::pair<int, float>& x, const std::pair<int, float>& y) { return x.first < y.first; });
       P.cell_slots[c].begin = slot;
-      size_t j = 0;
+      size_t j = 0;  // window position of the sender (senders ascending)
       for (size_t k = 0; k < snd.size(); k += kLaneEdges) {
         LaneChunk ch;
         ch.recv = r;
         ch.slot = slot++;
         for (size_t q = k; q < std::min(snd.size(), k + kLaneEdges); ++q) {
           const int s = snd[q].first;
-          while (s >= thi[j]) ++j;
-          ch.e.push_back({(uint16_t)(L.tiles + sizeof(float) * (size_t)(toff[j] + s - tlo[j])), snd[q].second});
+          while (u[j] < s) ++j;
+          ch.e.push_back({(uint16_t)(L.tiles + sizeof(float) * j), snd[q].second});
         }
         lc.push_back(std::move(ch));
       }
@@ -851,14 +843,11 @@ bool make_plan(const PlanInput& in, Plan* out, std::string* err) {
   res.res_edges = std::max(me, 1);
   if (!in.no_resident && smem_layout(res).total <= in.smem_budget) sh = res;
 
-  // ---- stamped exchange when every CTA's tiles fit in shared memory at once
+  // ---- stamped exchange when every CTA's window (its unique senders, one
+  // word each) fits in shared memory at once
   if (in.sync_mode != kSyncBarrier) {
     int sum_max = 4;
-    for (const CtaWork& w : P.cta) {
-      int s = 0;
-      for (int j = 0; j < w.n_tiles; ++j) s += P.tiles[w.tile_begin + j].nfloats;
-      sum_max = std::max(sum_max, s);
-    }
+    for (int b = 0; b < ctas; ++b) sum_max = std::max(sum_max, (int)uniq[b].size());
     // stamped plans keep their work resident in the packed lane-chunk layout,
     // 16-bit byte offsets from the start of dynamic shared memory (so every
     // offset must stay below 64 KiB)
@@ -878,11 +867,11 @@ bool make_plan(const PlanInput& in, Plan* out, std::string* err) {
       const bool offsets_fit = SL0.vown + sizeof(float) * (size_t)cells_cap <= 65536;
       if (in.no_resident || !offsets_fit) continue;
       packed = P;
-      pack_groups(packed, SL0, in, starts, st.dup_words);
+      pack_groups(packed, SL0, in, uniq, st.dup_words);
       int mg = 1;
       for (const CtaWork& w : packed.cta) mg = std::max(mg, w.n_groups);
       st.max_slots = packed.max_slots;
-      st.res_tiles = std::max(mt, 1);
+      st.res_tiles = (sum_max + 3) / 4;  // the window's cell ids, four per 16-byte descriptor slot
       st.res_chunks = mg * 32;
       st.res_edges = mg * kGroupEntries;
       fits = smem_layout(st).total <= in.smem_budget;
@@ -895,22 +884,24 @@ bool make_plan(const PlanInput& in, Plan* out, std::string* err) {
       P.edges.swap(packed.edges);
       P.edge_g.swap(packed.edge_g);
       P.max_slots = packed.max_slots;
+      // the windows replace the tiles: CTA b's window is gcol[tile_begin ..
+      // tile_begin + n_tiles), its unique senders in ascending order
+      P.tiles.clear();
+      P.chunks.clear();
+      P.gcol.clear();
+      for (int b = 0; b < ctas; ++b) {
+        CtaWork& w = P.cta[b];
+        w.tile_begin = (int)P.gcol.size();
+        w.n_tiles = (int)uniq[b].size();
+        P.gcol.insert(P.gcol.end(), uniq[b].begin(), uniq[b].end());
+      }
       // progress probes: CTAs that read a CTA's cells without being read by it
       std::vector<int> owner(n);
       for (int b = 0; b < ctas; ++b)
         for (int c = starts[b]; c < starts[b + 1]; ++c) owner[c] = b;
       std::vector<std::vector<char>> reads(ctas, std::vector<char>(ctas, 0));  // reads[r][x]: r polls x
-      for (int b = 0; b < ctas; ++b) {
-        const CtaWork& w = P.cta[b];
-        for (int j = 0; j < w.n_tiles; ++j) {
-          const TileDesc& td = P.tiles[w.tile_begin + j];
-          for (int c = td.lo; c < td.lo + td.nfloats && c < n;) {
-            const int x = owner[c];
-            reads[b][x] = 1;
-            c = starts[x + 1];  // skip to the next owner
-          }
-        }
-      }
+      for (int b = 0; b < ctas; ++b)
+        for (int c : uniq[b]) reads[b][owner[c]] = 1;
       for (int x = 0; x < ctas; ++x) {
         CtaWork& w = P.cta[x];
         w.probe_begin = (int)P.probes.size();
@@ -1044,18 +1035,18 @@ extern "C" int infoli_plan_emulate(int n, const int64_t* row_ptr, const int32_t*
     float* sVd = reinterpret_cast<float*>(sm.data() + L.vown);
     for (int r = 0; r < w.n_cells; ++r) sVd[r] = vdend[w.cell_begin + r];
     if (P.shape.stamped) {
-      size_t toff = 0;
-      for (int j = 0; j < w.n_tiles; ++j) {
-        const TileDesc& td = P.tiles[w.tile_begin + j];
-        const size_t dup = (size_t)P.shape.dup_words;
-        if (td.lo < 0 || td.lo % 4 || td.nfloats % 4 || dup + toff + td.nfloats > (size_t)P.shape.tile_cap ||
-            (dup && toff + td.nfloats > dup))
-          return -4;
-        for (int i = 0; i < td.nfloats; ++i) {
-          fsm[toff + i] = (td.lo + i < n) ? vdend[td.lo + i] : 0.0f;
-          if (dup) fsm[dup + toff + i] = fsm[toff + i];
-        }
-        toff += td.nfloats;
+      // the window: the CTA's unique senders, one float each (and the
+      // bank-shifted second copy), ids held four per descriptor slot
+      const size_t dup = (size_t)P.shape.dup_words;
+      const size_t nw = (size_t)w.n_tiles;
+      if (w.tile_begin < 0 || (size_t)w.tile_begin + nw > P.gcol.size() || dup + nw > (size_t)P.shape.tile_cap ||
+          (dup && nw > dup) || nw > (size_t)P.shape.res_tiles * 4)
+        return -4;
+      for (size_t i = 0; i < nw; ++i) {
+        const int c = P.gcol[(size_t)w.tile_begin + i];
+        if (c < 0 || c >= n || (i > 0 && c <= P.gcol[(size_t)w.tile_begin + i - 1])) return -4;
+        fsm[i] = vdend[c];
+        if (dup) fsm[dup + i] = fsm[i];
       }
       for (int q = 0; q < w.n_probes; ++q)
         if (P.probes[w.probe_begin + q] < 0 || P.probes[w.probe_begin + q] >= n) return -5;
