@@ -435,13 +435,26 @@ int infoli_run_noalloc(const float* params, int n_cells, const int64_t* d_row_pt
  * (sync_mode 0 auto, 1 grid barrier, 2 stamped words; grid 0 = automatic),
  * then computes the gap-junction currents of the voltages vdend[n] by walking
  * the plan's tables with the step kernel's addressing, every shared-memory
- * offset bounds-checked.  info[10] = {CTAs, stamped, tiles, chunks or groups,
- * partial slots, shared bytes, progress probes, resident, shared-memory
- * wavefronts of the stamped V_dend gathers, gather instructions}.  Returns 0
- * or a negative code naming the violated invariant. */
+ * offset bounds-checked.  info[10] = {CTAs, stamped, tiles (stamped plans: 1
+ * when the planner relabelled the cells), chunks or groups, partial slots,
+ * shared bytes, progress probes, resident, shared-memory wavefronts of the
+ * stamped V_dend gathers, gather instructions}.  vdend and ic_out are in the
+ * caller's cell order either way.  Returns 0 or a negative code naming the
+ * violated invariant. */
 int infoli_plan_emulate(int n, const int64_t* row_ptr, const int32_t* col, const float* g, float g_uniform,
                         int grid, int grid_max, int threads, int64_t smem_budget, int sync_mode,
                         const float* vdend, float* ic_out, int64_t info[10]);
+
+/* The planner's locality-preserving cell order (no counterpart in the
+ * reference).  Stamped plans whose windows are wide are re-planned in this
+ * order: spectral coordinates of the cells (the two lowest non-trivial
+ * eigenvectors of the in-edge graph Laplacian) cut into `parts` compact
+ * blocks of at most `threads` cells by recursive coordinate bisection.
+ * order[new] = old cell id, starts[parts + 1] = the blocks in the new order.
+ * The caller's cell order stays the order of every array at this interface.
+ * Returns 0, or -1 when no such order exists (e.g. too few cells). */
+int infoli_plan_locality_order(int n, const int64_t* row_ptr, const int32_t* col, int parts, int threads,
+                               int32_t* order, int32_t* starts);
 
 /* ------------------------------------------------------------------------ */
 /* trace text (host side)                                                    */

@@ -40,7 +40,7 @@ EXPORTED = [
     "infoli_sim_set_stimulus_pulse", "infoli_sim_set_stimulus_cells", "infoli_sim_run",
     "infoli_sim_run_into", "infoli_sim_get_state", "infoli_sim_set_state", "infoli_sim_step",
     "infoli_sim_last_run_stats", "infoli_sim_plan_info", "infoli_sim_destroy", "infoli_format_f8",
-    "infoli_format_row", "infoli_sim_set_profiling", "infoli_sim_get_profile", "infoli_plan_emulate",
+    "infoli_format_row", "infoli_sim_set_profiling", "infoli_sim_get_profile", "infoli_plan_emulate", "infoli_plan_locality_order",
     "infoli_run_noalloc", "infoli_sim_launch", "infoli_sim_query", "infoli_sim_sync",
     "infoli_sim_memory", "infoli_gen_bitmask_csr",
     "infoli_read_conn_dense", "infoli_read_conn_triples", "infoli_read_stim_file", "infoli_random_init",
@@ -175,6 +175,7 @@ def load():
         "infoli_sim_sync": ([P], I),
         "infoli_sim_memory": ([P, P], I),
         "infoli_plan_emulate": ([I, P, P, P, F, I, I, I, I64, I, P, P, P], I),
+        "infoli_plan_locality_order": ([I, P, P, I, I, P, P], I),
         "infoli_run_noalloc": ([P, I, P, P, P, F, I, I, F, P, I, I, P, P], I),
         "infoli_sim_set_profiling": ([P, I], I),
         "infoli_sim_get_profile": ([P, P, P], I),
@@ -354,7 +355,22 @@ def plan_emulate(n, row_ptr, col, vdend, g=None, g_uniform=0.04, grid=0, grid_ma
         raise InfoliError(rc, f"plan emulation failed with code {rc}")
     keys = ("ctas", "stamped", "tiles", "chunks", "max_slots", "smem_bytes", "probes", "resident",
             "gather_wavefronts", "gathers")
-    return out, dict(zip(keys, info.tolist()))
+    d = dict(zip(keys, info.tolist()))
+    if d["stamped"] == 1:
+        d["relabelled"] = bool(d.pop("tiles"))
+    return out, d
+
+
+def plan_locality_order(n, row_ptr, col, parts, threads=512):
+    """The planner's locality-preserving cell order (infoli_plan_locality_order):
+    (order[new] = old cell, starts[parts + 1]) or None when no order exists."""
+    row_ptr = np.ascontiguousarray(row_ptr, dtype=np.int64)
+    col = np.ascontiguousarray(col, dtype=np.int32)
+    order = np.zeros(n, dtype=np.int32)
+    starts = np.zeros(parts + 1, dtype=np.int32)
+    rc = load().infoli_plan_locality_order(int(n), _p(row_ptr), _p(col) if col.size else None, int(parts),
+                                           int(threads), _p(order), _p(starts))
+    return None if rc != 0 else (order, starts)
 
 
 def device_count() -> int:

@@ -102,7 +102,8 @@ struct infoli_sim {
   float* d_edge_g = nullptr;
   int* d_probes = nullptr;
   int2_t* d_gdesc = nullptr;
-  int32_t* d_gcol = nullptr;  // gather plans
+  int32_t* d_gcol = nullptr;  // gather plans; stamped plans: window sender ids
+  int32_t* d_perm = nullptr;  // relabelled plans: caller's cell id of each plan cell
   unsigned long long* d_vll[2] = {nullptr, nullptr};  // stamped exchange words
   // state
   float* d_vd[2] = {nullptr, nullptr};
@@ -144,7 +145,7 @@ void release(infoli_sim* s) {
                    s->d_edge_g, s->d_vd[0], s->d_vd[1],  s->d_st,         s->d_ca,
                    s->d_cell_amp, s->d_cell_onset, s->d_bar, s->d_err, s->d_trace[0], s->d_trace[1],
                    s->d_prof, s->d_probes, s->d_vll[0], s->d_vll[1], s->d_gdesc, s->d_stim_table,
-                   s->d_gcol};
+                   s->d_gcol, s->d_perm};
   if (s->stream) {
     for (void* p : dptrs)
       if (p) cudaFreeAsync(p, s->stream);
@@ -227,6 +228,7 @@ int fill_args(infoli_sim* s, StepArgs* a) {
   a->probes = s->d_probes;
   a->gdesc = reinterpret_cast<const int2*>(s->d_gdesc);
   a->gcol = s->d_gcol;
+  a->perm = s->d_perm;
   a->n_cells = s->n;
   return INFOLI_OK;
 }
@@ -322,6 +324,7 @@ int infoli_sim_create(const infoli_sim_desc* d, infoli_sim** out) {
   pin.smem_budget = (size_t)smem_optin - 1024;  // static shared (abort flag) headroom
   pin.kahan = s->kahan;
   pin.no_resident = getenv("INFOLI_NO_RESIDENT") ? 1 : 0;
+  pin.reorder = getenv("INFOLI_NO_REORDER") ? 0 : 1;
   if (const char* sm = getenv("INFOLI_SYNC"))
     pin.sync_mode = !strcmp(sm, "barrier")   ? kSyncBarrier
                     : !strcmp(sm, "stamped") ? kSyncStamped
@@ -368,7 +371,8 @@ int infoli_sim_create(const infoli_sim_desc* d, infoli_sim** out) {
       (rc = dev_upload(&s->d_edge_g, s->plan.edge_g.data(), s->plan.edge_g.size(), dv, st0)) ||
       (rc = dev_upload(&s->d_probes, s->plan.probes.data(), s->plan.probes.size(), dv, st0)) ||
       (rc = dev_upload(&s->d_gdesc, s->plan.gdesc.data(), s->plan.gdesc.size(), dv, st0)) ||
-      (rc = dev_upload(&s->d_gcol, s->plan.gcol.data(), s->plan.gcol.size(), dv, st0)))
+      (rc = dev_upload(&s->d_gcol, s->plan.gcol.data(), s->plan.gcol.size(), dv, st0)) ||
+      (rc = dev_upload(&s->d_perm, s->plan.perm.data(), s->plan.perm.size(), dv, st0)))
     return fail(rc);
   // the kernel needs valid pointers even for empty tables
   if ((!s->d_chunks && pool_alloc(&s->d_chunks, sizeof(ChunkDesc), dv, st0) != cudaSuccess) ||

@@ -358,7 +358,10 @@ __global__ void __launch_bounds__(BLOCK, 1) step_kernel(const __grid_constant__ 
   const int warp = tid >> 5;
   const int nwarps = blockDim.x >> 5;
   const bool owner = tid < w.n_cells;  // voltage thread of cell w.cell_begin + tid
-  const int cell = w.cell_begin + tid;
+  const int cell = w.cell_begin + tid;  // plan cell id (exchange words, plan tables)
+  // the caller's id of the cell (state, inputs, traces); plans relabel only
+  // stamped exchanges, whose V_dend words are the vll arrays
+  const int ocell = (a.perm && owner) ? a.perm[cell] : cell;
   const long long np = a.n_pad;
   const int tile_cap = shp.tile_cap;
   const int nbuf = shp.nbuf;
@@ -468,8 +471,8 @@ __global__ void __launch_bounds__(BLOCK, 1) step_kernel(const __grid_constant__ 
   double* sCa = reinterpret_cast<double*>(smem_raw + L.gca);
   if (owner) {
     const float* st = a.st;
-    for (int f = F_Q; f < F_COUNT; ++f) sG[f * cap + tid] = st[f * np + cell];
-    sCa[tid] = a.ca[cell];
+    for (int f = F_Q; f < F_COUNT; ++f) sG[f * cap + tid] = st[f * np + ocell];
+    sCa[tid] = a.ca[ocell];
   }
   // voltage threads hold the per-cell constants of the voltage step
   int2 slots = make_int2(0, 0);
@@ -477,16 +480,16 @@ __global__ void __launch_bounds__(BLOCK, 1) step_kernel(const __grid_constant__ 
   float my_amp = 0.0f;
   int my_onset = 0, my_off = 0;
   if (owner) {
-    sVd[tid] = a.vd[a.step0 & 1][cell];
-    sVs[tid] = a.st[F_VS * np + cell];
-    sVa[tid] = a.st[F_VA * np + cell];
+    sVd[tid] = a.vd[a.step0 & 1][ocell];
+    sVs[tid] = a.st[F_VS * np + ocell];
+    sVa[tid] = a.st[F_VA * np + ocell];
     slots = a.cell_slots[cell];
-    if (a.cell_g) gscale = a.cell_g[cell];
+    if (a.cell_g) gscale = a.cell_g[ocell];
     if (a.stim_kind == STIM_CELL) {
-      my_amp = a.cell_amp[cell];
-      my_onset = a.cell_onset[cell];
+      my_amp = a.cell_amp[ocell];
+      my_onset = a.cell_onset[ocell];
     }
-    if (a.cell_step_off) my_off = a.cell_step_off[cell];
+    if (a.cell_step_off) my_off = a.cell_step_off[ocell];
   }
   const VoltCoef vk = volt_coef(a.P);
   const bool prof = a.prof != nullptr && tid == 0;
@@ -626,7 +629,7 @@ __global__ void __launch_bounds__(BLOCK, 1) step_kernel(const __grid_constant__ 
       else if (a.stim_kind == STIM_CELL)
         iapp = (ls >= my_onset && ls < my_onset + a.stim_dur) ? my_amp : 0.0f;
       else
-        iapp = a.stim_table[(size_t)t * np + cell];
+        iapp = a.stim_table[(size_t)t * np + ocell];
       Currents cur;
       cur.I_h = sI[0 * cap + tid];
       cur.I_CaH = sI[1 * cap + tid];
@@ -650,7 +653,7 @@ __global__ void __launch_bounds__(BLOCK, 1) step_kernel(const __grid_constant__ 
       sVs[tid] = v.Vs;
       sVa[tid] = v.Va;
       if (a.trace_every > 0 && (step % a.trace_every) == 0) {
-        float* tr = a.trace + (size_t)row * a.trace_nq * np + cell;
+        float* tr = a.trace + (size_t)row * a.trace_nq * np + ocell;
         int qi = 0;
         if (a.trace_mask & TRACE_AXON) tr[(qi++) * np] = v.Va;
         if (a.trace_mask & TRACE_SOMA) tr[(qi++) * np] = v.Vs;
@@ -704,11 +707,11 @@ __global__ void __launch_bounds__(BLOCK, 1) step_kernel(const __grid_constant__ 
 
   if (owner) {
     float* st = a.st;
-    for (int f = F_Q; f < F_COUNT; ++f) st[f * np + cell] = sG[f * cap + tid];
-    a.ca[cell] = sCa[tid];
-    if (LL) a.vd[(a.step0 + a.n_steps) & 1][cell] = sVd[tid];
-    st[F_VS * np + cell] = sVs[tid];
-    st[F_VA * np + cell] = sVa[tid];
+    for (int f = F_Q; f < F_COUNT; ++f) st[f * np + ocell] = sG[f * cap + tid];
+    a.ca[ocell] = sCa[tid];
+    if (LL) a.vd[(a.step0 + a.n_steps) & 1][ocell] = sVd[tid];
+    st[F_VS * np + ocell] = sVs[tid];
+    st[F_VA * np + ocell] = sVa[tid];
   }
 }
 

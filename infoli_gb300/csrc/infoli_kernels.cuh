@@ -39,6 +39,8 @@ struct StepArgs {
   const uint16_t* edges;      // tile-relative sender offsets
   const float* edge_g;        // per-edge conductance (same order) or nullptr
   const int* gcol;            // gather plans: sender ids, column by column per CTA
+  const int* perm;            // relabelled stamped plans: caller's cell id of plan cell i
+                              // (state, inputs and traces are in the caller's order); null = same
   const float* cell_g;        // per-cell conductance scale (uniform per network) or nullptr
   float g_uniform;            // used when edge_g and cell_g are both null
   // state

@@ -582,7 +582,7 @@ static bool make_bits_plan(const PlanInput& in, Plan* out, std::string* err) {
   return true;
 }
 
-bool make_plan(const PlanInput& in, Plan* out, std::string* err) {
+bool make_plan_base(const PlanInput& in, Plan* out, std::string* err) {
   const int n = in.n;
   if (n <= 0 || !in.row_ptr || in.threads <= 0 || in.threads % 32 || in.grid_max <= 0) {
     *err = "make_plan: bad input";
@@ -628,7 +628,8 @@ bool make_plan(const PlanInput& in, Plan* out, std::string* err) {
     *err = "make_plan: network larger than the co-resident thread count";
     return false;
   }
-  std::vector<int> starts = partition_cells(n, in.row_ptr, grid, threads);
+  std::vector<int> starts = in.cta_starts ? std::vector<int>(in.cta_starts, in.cta_starts + grid + 1)
+                                          : partition_cells(n, in.row_ptr, grid, threads);
   const int ctas = (int)starts.size() - 1;
   int cells_cap = 32;
   for (int b = 0; b < ctas; ++b) cells_cap = std::max(cells_cap, ((starts[b + 1] - starts[b] + 31) / 32) * 32);
@@ -928,6 +929,248 @@ bool make_plan(const PlanInput& in, Plan* out, std::string* err) {
   return true;
 }
 
+namespace {
+
+uint64_t splitmix64(uint64_t* x) {
+  uint64_t z = (*x += 0x9e3779b97f4a7c15ull);
+  z = (z ^ (z >> 30)) * 0xbf58476d1ce4e5b9ull;
+  z = (z ^ (z >> 27)) * 0x94d049bb133111ebull;
+  return z ^ (z >> 31);
+}
+
+// Eigen-decomposition of a symmetric 3x3 matrix by cyclic Jacobi rotations:
+// eigenvalues in w, eigenvectors in the columns of V.
+void jacobi3(double A[3][3], double w[3], double V[3][3]) {
+  for (int i = 0; i < 3; ++i)
+    for (int j = 0; j < 3; ++j) V[i][j] = i == j ? 1.0 : 0.0;
+  for (int sweep = 0; sweep < 50; ++sweep) {
+    const double off = A[0][1] * A[0][1] + A[0][2] * A[0][2] + A[1][2] * A[1][2];
+    if (off < 1e-30) break;
+    for (int p = 0; p < 2; ++p)
+      for (int q = p + 1; q < 3; ++q) {
+        if (std::fabs(A[p][q]) < 1e-300) continue;
+        const double theta = (A[q][q] - A[p][p]) / (2.0 * A[p][q]);
+        const double t = (theta >= 0 ? 1.0 : -1.0) / (std::fabs(theta) + std::sqrt(theta * theta + 1.0));
+        const double c = 1.0 / std::sqrt(t * t + 1.0), sn = t * c;
+        for (int k = 0; k < 3; ++k) {  // A <- A J
+          const double akp = A[k][p], akq = A[k][q];
+          A[k][p] = c * akp - sn * akq;
+          A[k][q] = sn * akp + c * akq;
+        }
+        for (int k = 0; k < 3; ++k) {  // A <- J^T A
+          const double apk = A[p][k], aqk = A[q][k];
+          A[p][k] = c * apk - sn * aqk;
+          A[q][k] = sn * apk + c * aqk;
+        }
+        for (int k = 0; k < 3; ++k) {
+          const double vkp = V[k][p], vkq = V[k][q];
+          V[k][p] = c * vkp - sn * vkq;
+          V[k][q] = sn * vkp + c * vkq;
+        }
+      }
+  }
+  for (int i = 0; i < 3; ++i) w[i] = A[i][i];
+}
+
+int max_window(const Plan& P) {
+  int m = 0;
+  for (const CtaWork& w : P.cta) m = std::max(m, w.n_tiles);
+  return m;
+}
+
+}  // namespace
+
+// Spectral coordinates: the two lowest non-trivial eigenvectors of the
+// in-edge graph Laplacian L = D - A (D = in-degrees), by subspace iteration
+// with three vectors on (c I - L), c = 2 max degree + 1, deflating the
+// constant vector every step, then a Rayleigh-Ritz step.  On graphs whose
+// edges join nearby cells (distance-dependent connectivity) these
+// coordinates follow the cells' positions.  Recursive coordinate bisection
+// of them (along the wider extent, balanced by the planner's CTA cost) gives
+// `parts` compact blocks; cells keep ascending ids inside a block.
+std::vector<int> locality_order(const PlanInput& in, int parts, int threads, std::vector<int>* starts) {
+  const int n = in.n;
+  std::vector<int> order;
+  if (n < 8 || parts < 2 || (int64_t)parts * threads < n) return order;
+  double dmax = 0.0;
+  for (int i = 0; i < n; ++i) dmax = std::max(dmax, (double)(in.row_ptr[i + 1] - in.row_ptr[i]));
+  const double cshift = 2.0 * dmax + 1.0;
+  std::vector<double> X((size_t)n * 3), Y((size_t)n * 3);
+  uint64_t rs = 0x5eed5eedull;
+  for (double& x : X) x = (double)(splitmix64(&rs) >> 11) * (2.0 / 9007199254740992.0) - 1.0;
+  auto deflate = [&](std::vector<double>& M) {
+    for (int k = 0; k < 3; ++k) {
+      double m = 0.0;
+      for (int i = 0; i < n; ++i) m += M[(size_t)i * 3 + k];
+      m /= n;
+      for (int i = 0; i < n; ++i) M[(size_t)i * 3 + k] -= m;
+    }
+  };
+  auto apply_L = [&](const std::vector<double>& Xi, std::vector<double>& Yo, double shift) {
+    // Yo = shift * Xi - L Xi
+#pragma omp parallel for schedule(static)
+    for (int i = 0; i < n; ++i) {
+      double s0 = 0.0, s1 = 0.0, s2 = 0.0;
+      for (int64_t e = in.row_ptr[i]; e < in.row_ptr[i + 1]; ++e) {
+        const size_t j = (size_t)in.col[e] * 3;
+        s0 += Xi[j];
+        s1 += Xi[j + 1];
+        s2 += Xi[j + 2];
+      }
+      const double d = (double)(in.row_ptr[i + 1] - in.row_ptr[i]);
+      const size_t o = (size_t)i * 3;
+      Yo[o] = shift * Xi[o] - (d * Xi[o] - s0);
+      Yo[o + 1] = shift * Xi[o + 1] - (d * Xi[o + 1] - s1);
+      Yo[o + 2] = shift * Xi[o + 2] - (d * Xi[o + 2] - s2);
+    }
+  };
+  auto orthonormalize = [&](std::vector<double>& M) {
+    for (int k = 0; k < 3; ++k) {
+      for (int q = 0; q < k; ++q) {
+        double dot = 0.0;
+        for (int i = 0; i < n; ++i) dot += M[(size_t)i * 3 + k] * M[(size_t)i * 3 + q];
+        for (int i = 0; i < n; ++i) M[(size_t)i * 3 + k] -= dot * M[(size_t)i * 3 + q];
+      }
+      double nrm = 0.0;
+      for (int i = 0; i < n; ++i) nrm += M[(size_t)i * 3 + k] * M[(size_t)i * 3 + k];
+      nrm = std::sqrt(nrm);
+      if (nrm < 1e-300) return false;
+      for (int i = 0; i < n; ++i) M[(size_t)i * 3 + k] /= nrm;
+    }
+    return true;
+  };
+  deflate(X);
+  if (!orthonormalize(X)) return order;
+  for (int it = 0; it < kReorderIters; ++it) {
+    apply_L(X, Y, cshift);
+    deflate(Y);
+    if (!orthonormalize(Y)) return order;
+    X.swap(Y);
+  }
+  // Rayleigh-Ritz: H = X^T L X (Y = -L X with shift 0)
+  apply_L(X, Y, 0.0);
+  double H[3][3], w[3], V[3][3];
+  for (int a = 0; a < 3; ++a)
+    for (int b = 0; b < 3; ++b) {
+      double h = 0.0;
+      for (int i = 0; i < n; ++i) h -= X[(size_t)i * 3 + a] * Y[(size_t)i * 3 + b];
+      H[a][b] = h;
+    }
+  for (int a = 0; a < 3; ++a)
+    for (int b = a + 1; b < 3; ++b) H[a][b] = H[b][a] = 0.5 * (H[a][b] + H[b][a]);
+  jacobi3(H, w, V);
+  int idx[3] = {0, 1, 2};
+  std::sort(idx, idx + 3, [&](int p, int q) { return w[p] < w[q]; });
+  std::vector<double> C((size_t)n * 2);
+  for (int i = 0; i < n; ++i)
+    for (int k = 0; k < 2; ++k) {
+      double v = 0.0;
+      for (int a = 0; a < 3; ++a) v += X[(size_t)i * 3 + a] * V[a][idx[k]];
+      C[(size_t)i * 2 + k] = v;
+    }
+  // recursive coordinate bisection, balanced by the CTA cost
+  std::vector<int64_t> cost(n);
+  for (int i = 0; i < n; ++i) cost[i] = (in.row_ptr[i + 1] - in.row_ptr[i]) + kCellCost;
+  std::vector<int> ids(n);
+  for (int i = 0; i < n; ++i) ids[i] = i;
+  order.reserve(n);
+  starts->assign(1, 0);
+  struct Range {
+    int lo, hi, parts;
+  };
+  std::vector<Range> stack{{0, n, parts}};
+  while (!stack.empty()) {
+    const Range r = stack.back();
+    stack.pop_back();
+    if (r.parts == 1 || r.hi - r.lo <= 1) {
+      if (r.hi - r.lo > threads) {
+        order.clear();
+        return order;
+      }
+      std::sort(ids.begin() + r.lo, ids.begin() + r.hi);
+      order.insert(order.end(), ids.begin() + r.lo, ids.begin() + r.hi);
+      starts->push_back((int)order.size());
+      // a leaf of several parts with one cell: the remaining parts stay empty
+      continue;
+    }
+    double lo0 = 1e300, hi0 = -1e300, lo1 = 1e300, hi1 = -1e300;
+    for (int k = r.lo; k < r.hi; ++k) {
+      const double* c = &C[(size_t)ids[k] * 2];
+      lo0 = std::min(lo0, c[0]);
+      hi0 = std::max(hi0, c[0]);
+      lo1 = std::min(lo1, c[1]);
+      hi1 = std::max(hi1, c[1]);
+    }
+    const int ax = (hi0 - lo0) >= (hi1 - lo1) ? 0 : 1;
+    std::stable_sort(ids.begin() + r.lo, ids.begin() + r.hi, [&](int p, int q) {
+      const double a = C[(size_t)p * 2 + ax], b = C[(size_t)q * 2 + ax];
+      return a < b || (a == b && p < q);
+    });
+    const int p1 = r.parts / 2;
+    int64_t total = 0;
+    for (int k = r.lo; k < r.hi; ++k) total += cost[ids[k]];
+    const double target = (double)total * p1 / r.parts;
+    int64_t acc = 0;
+    int cut = r.lo;
+    while (cut < r.hi - 1 && (double)(acc + cost[ids[cut]]) <= target) acc += cost[ids[cut++]];
+    if (cut == r.lo) ++cut;
+    // second half pushed first, so the first half is emitted first
+    stack.push_back({cut, r.hi, r.parts - p1});
+    stack.push_back({r.lo, cut, p1});
+  }
+  if ((int)order.size() != n) order.clear();
+  return order;
+}
+
+// Plans the network as given; for stamped plans with wide windows, also
+// plans it in a locality-preserving cell order and keeps that plan when its
+// largest window is at least a fifth smaller.
+bool make_plan(const PlanInput& in, Plan* out, std::string* err) {
+  if (!make_plan_base(in, out, err)) return false;
+  if (!in.reorder || in.cta_starts || !out->shape.stamped || out->cta.size() < 2) return true;
+  const int n = in.n;
+  const int ctas = (int)out->cta.size();
+  const int64_t E = in.row_ptr[n];
+  const int w0 = max_window(*out);
+  const int per_cta = (n + ctas - 1) / ctas;
+  if (E > kReorderMaxEdges || w0 > n / 2 || w0 < kReorderMinWindowRatio * per_cta) return true;
+  std::vector<int> starts;
+  std::vector<int> order = locality_order(in, ctas, in.threads, &starts);
+  if (order.empty() || (int)starts.size() != ctas + 1) return true;
+  std::vector<int> inv(n);
+  for (int i = 0; i < n; ++i) inv[order[i]] = i;
+  std::vector<int64_t> rp(n + 1, 0);
+  std::vector<int32_t> col((size_t)E);
+  std::vector<float> g(in.g ? (size_t)E : 0);
+  for (int r = 0; r < n; ++r) rp[r + 1] = rp[r] + (in.row_ptr[order[r] + 1] - in.row_ptr[order[r]]);
+#pragma omp parallel for schedule(dynamic, 64)
+  for (int r = 0; r < n; ++r) {
+    const int o = order[r];
+    std::vector<std::pair<int, float>> e;
+    e.reserve((size_t)(in.row_ptr[o + 1] - in.row_ptr[o]));
+    for (int64_t k = in.row_ptr[o]; k < in.row_ptr[o + 1]; ++k) e.push_back({inv[in.col[k]], in.g ? in.g[k] : 0.0f});
+    std::stable_sort(e.begin(), e.end(),
+                     [](const std::pair<int, float>& x, const std::pair<int, float>& y) { return x.first < y.first; });
+    for (size_t k = 0; k < e.size(); ++k) {
+      col[(size_t)rp[r] + k] = e[k].first;
+      if (in.g) g[(size_t)rp[r] + k] = e[k].second;
+    }
+  }
+  PlanInput in2 = in;
+  in2.row_ptr = rp.data();
+  in2.col = col.data();
+  in2.g = in.g ? g.data() : nullptr;
+  in2.grid = ctas;
+  in2.cta_starts = starts.data();
+  Plan P2;
+  std::string e2;
+  if (!make_plan_base(in2, &P2, &e2) || !P2.shape.stamped || (int)P2.cta.size() != ctas) return true;
+  if ((int64_t)max_window(P2) * 5 > (int64_t)w0 * 4) return true;
+  P2.perm.assign(order.begin(), order.end());
+  *out = std::move(P2);
+  return true;
+}
+
 }  // namespace infoli
 
 // ---------------------------------------------------------------------------
@@ -939,7 +1182,7 @@ bool make_plan(const PlanInput& in, Plan* out, std::string* err) {
 // CPU test suite to validate the planner without a GPU.
 extern "C" int infoli_plan_emulate(int n, const int64_t* row_ptr, const int32_t* col, const float* g,
                                    float g_uniform, int grid, int grid_max, int threads, int64_t smem_budget,
-                                   int sync_mode, const float* vdend, float* ic_out, int64_t info[10]) {
+                                   int sync_mode, const float* vdend_in, float* ic_out_in, int64_t info[10]) {
   using namespace infoli;
   PlanInput in;
   in.n = n;
@@ -954,6 +1197,24 @@ extern "C" int infoli_plan_emulate(int n, const int64_t* row_ptr, const int32_t*
   Plan P;
   std::string err;
   if (!make_plan(in, &P, &err)) return -1;
+  // relabelled plans: evaluate in plan order, report in the caller's order
+  std::vector<float> v_plan, ic_plan;
+  const float* vdend = vdend_in;
+  float* ic_out = ic_out_in;
+  if (!P.perm.empty()) {
+    if ((int)P.perm.size() != n) return -9;
+    std::vector<char> seen(n, 0);
+    v_plan.resize(n);
+    ic_plan.assign(n, 0.0f);
+    for (int i = 0; i < n; ++i) {
+      const int o = P.perm[i];
+      if (o < 0 || o >= n || seen[o]) return -9;
+      seen[o] = 1;
+      v_plan[i] = vdend_in[o];
+    }
+    vdend = v_plan.data();
+    ic_out = ic_plan.data();
+  }
   const SmemLayout L = smem_layout(P.shape);
   if (P.shape.gather >= 2 ? tgather_smem_bytes(P.shape) > (size_t)smem_budget
                           : !P.shape.gather && L.total > (size_t)smem_budget)
@@ -1112,10 +1373,12 @@ extern "C" int infoli_plan_emulate(int n, const int64_t* row_ptr, const int32_t*
       ic_out[w.cell_begin + r] = g ? ic : ic * g_uniform;
     }
   }
+  if (!P.perm.empty())
+    for (int i = 0; i < n; ++i) ic_out_in[P.perm[i]] = ic_plan[i];
   if (info) {
     info[0] = P.grid;
     info[1] = P.shape.gather ? 1 + P.shape.gather : P.shape.stamped;
-    info[2] = (int64_t)P.tiles.size();
+    info[2] = P.shape.stamped ? (int64_t)!P.perm.empty() : (int64_t)P.tiles.size();
     info[3] = P.shape.stamped ? groups : (int64_t)P.chunks.size();
     info[4] = P.shape.max_slots;
     info[5] = (int64_t)P.smem_bytes;
@@ -1124,5 +1387,25 @@ extern "C" int infoli_plan_emulate(int n, const int64_t* row_ptr, const int32_t*
     info[8] = gather_waves;
     info[9] = gathers;
   }
+  return 0;
+}
+
+// The planner's locality-preserving cell order (see locality_order): order[new]
+// = old cell, starts = the CTA ranges in the new order (parts + 1 entries).
+// Returns 0, or -1 when no order was found.
+extern "C" int infoli_plan_locality_order(int n, const int64_t* row_ptr, const int32_t* col, int parts,
+                                          int threads, int32_t* order_out, int32_t* starts_out) {
+  using namespace infoli;
+  if (n <= 0 || !row_ptr || (row_ptr[n] > 0 && !col) || parts < 1 || threads < 1 || !order_out || !starts_out)
+    return -1;
+  PlanInput in;
+  in.n = n;
+  in.row_ptr = row_ptr;
+  in.col = col;
+  std::vector<int> starts;
+  const std::vector<int> order = locality_order(in, parts, threads, &starts);
+  if ((int)order.size() != n || (int)starts.size() != parts + 1) return -1;
+  for (int i = 0; i < n; ++i) order_out[i] = order[i];
+  for (int i = 0; i <= parts; ++i) starts_out[i] = starts[i];
   return 0;
 }

@@ -35,7 +35,16 @@ struct PlanInput {
   int kahan = 0;
   int no_resident = 0;             // force per-step reads of the static work from global memory
   int sync_mode = 0;               // kSyncAuto / kSyncBarrier / kSyncStamped
+  int reorder = 1;                 // stamped plans: try a locality-preserving cell order
+  const int* cta_starts = nullptr; // optional CTA cell ranges (grid + 1 entries; internal)
 };
+
+// Locality reordering is tried for stamped plans whose largest window is at
+// least kReorderMinWindowRatio x the cells per CTA and at most half the
+// network, on networks of at most kReorderMaxEdges edges; it is kept when it
+// shrinks the largest window by at least a fifth.
+enum { kReorderMinWindowRatio = 4, kReorderIters = 160 };
+constexpr int64_t kReorderMaxEdges = 32ll << 20;
 
 enum { kSyncAuto = 0, kSyncBarrier = 1, kSyncStamped = 2, kSyncGather = 3, kSyncTiledGather = 4, kSyncBits = 5 };
 
@@ -62,6 +71,9 @@ struct Plan {
   std::vector<int32_t> gcol;          // gather mode: sender ids, column by column per CTA;
                                       // tiled gather: entries per (tile, receiver);
                                       // bitmask plans: the rows' bit words
+  std::vector<int32_t> perm;          // relabelled plans: perm[plan cell] = caller's cell
+                                      // (empty: the caller's order); every table above
+                                      // uses plan cell ids
 };
 
 // Shared-memory bytes the step kernel needs for a plan's parameters.
@@ -69,5 +81,10 @@ size_t plan_smem_bytes(int tile_cap, int nbuf, int threads, int cells_cap, int m
 
 // Returns false and sets *err on failure.
 bool make_plan(const PlanInput& in, Plan* out, std::string* err);
+
+// Locality-preserving cell order for `parts` CTAs of at most `threads`
+// cells: order[new] = old and the CTA starts in the new order (parts + 1
+// entries).  Empty when no such order was found.
+std::vector<int> locality_order(const PlanInput& in, int parts, int threads, std::vector<int>* starts);
 
 }  // namespace infoli

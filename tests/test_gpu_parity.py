@@ -318,3 +318,49 @@ def test_batch_with_tiny_networks(ig, conf):
             s = np.ascontiguousarray(bt.net_state(st0, i)).copy()
             O.run(n, conf[:23], s, rp, col, g_uniform=g, nsteps=300, trace_every=0, traces=())
             assert np.max(np.abs(bt.net_state(got, i)[O.S["V_soma"]] - s[O.S["V_soma"]])) <= TOL_VSOMA_MV
+
+
+@pytest.mark.parametrize("stim_kind", ["cell", "table"])
+def test_relabelled_stamped_plan_matches_oracle(ig, conf, stim_kind, monkeypatch):
+    """A 60 x 60 Gaussian grid whose stamped plan runs in the planner's
+    locality order: per-edge g, per-cell pulses or a per-step stimulus table,
+    traces and the final state all stay in the caller's cell order.  The run
+    without relabelling agrees within the same tolerance."""
+    from infoli_gb300 import capi
+
+    n = 3600
+    rp, col = ig.gen_grid_gaussian(60, 60, 6.0, 11.0, 4)
+    g = np.random.default_rng(3).uniform(0.02, 0.06, len(col)).astype(np.float32)
+    v = np.full(n, -60.0, dtype=np.float32)
+    assert capi.plan_emulate(n, rp, col, v, g=g, threads=512)[1]["relabelled"]
+    steps = 2000
+    rng = np.random.default_rng(11)
+    if stim_kind == "cell":
+        stim = ("cell", rng.uniform(0.0, 1.0, n).astype(np.float32), rng.integers(0, 1500, n).astype(np.int32), 100)
+    else:
+        stim = ("table", rng.uniform(-0.5, 0.5, (steps, n)).astype(np.float32), 0)
+    st0 = hetero_state(conf, n, 12)
+
+    def gpu_run():
+        sim = ig.Simulation(n, conf, rp, col, g=g, init_state=st0)
+        if stim_kind == "cell":
+            sim.set_stimulus_cells(stim[1], stim[2], stim[3])
+        else:
+            sim.set_stimulus_table(stim[1])
+        tr = sim.run(steps, 1, ALL)
+        fin = sim.get_state()
+        sim.close()
+        return tr, fin
+
+    gpu, final = gpu_run()
+    st = st0.copy()
+    ref = O.run(n, conf[:23], st, rp, col, g=g, stim=stim, nsteps=steps, trace_every=1, nthreads=8)
+    assert np.max(np.abs(gpu["soma"] - ref["soma"])) <= TOL_VSOMA_MV
+    # a cell mapped to another cell's state would be off by up to ~2 mV (the
+    # initial V_dend spread) or by a pulse; 5e-3 bounds the FP32 drift
+    for q in ("axon", "dend"):
+        assert np.max(np.abs(gpu[q] - ref[q])) <= 5e-3, q
+    assert np.max(np.abs(final - st)) <= 5e-3
+    monkeypatch.setenv("INFOLI_NO_REORDER", "1")
+    plain, _ = gpu_run()
+    assert np.max(np.abs(plain["soma"] - gpu["soma"])) <= TOL_VSOMA_MV

@@ -140,3 +140,49 @@ def test_bitmask_plans(capi):
     with pytest.raises(capi.InfoliError):
         capi.plan_emulate(100, *capi.gen_fixed_degree(100, 5, 1, (0.02, 0.06))[:2], np.zeros(100, np.float32),
                           g=np.full(500, 0.04, np.float32), sync_mode=5)
+
+
+def _windows(rp, col, order, starts):
+    """Unique senders of each block of cells order[starts[b]:starts[b+1]]."""
+    out = []
+    for b in range(len(starts) - 1):
+        cells = order[starts[b]:starts[b + 1]]
+        idx = np.concatenate([np.arange(rp[c], rp[c + 1]) for c in cells]) if len(cells) else np.zeros(0, int)
+        out.append(len(np.unique(col[idx])))
+    return np.array(out)
+
+
+def test_locality_order_compacts_grid_windows(capi):
+    """Spectral order + recursive bisection on a 60 x 60 Gaussian grid: a valid
+    permutation into 152 blocks of at most 512 cells whose sender windows are
+    far narrower than those of contiguous ranges of the caller's order."""
+    n, parts = 3600, 152
+    rp, col = capi.gen_grid_gaussian(60, 60, 6.0, 11.0, 4)
+    rp, col = np.asarray(rp), np.asarray(col)
+    order, starts = capi.plan_locality_order(n, rp, col, parts, 512)
+    assert np.array_equal(np.sort(order), np.arange(n))
+    assert starts[0] == 0 and starts[-1] == n and np.all(np.diff(starts) >= 1) and np.all(np.diff(starts) <= 512)
+    w_new = _windows(rp, col, order, starts)
+    w_old = _windows(rp, col, np.arange(n), np.linspace(0, n, parts + 1).astype(int))
+    assert w_new.max() * 1.5 < w_old.max() and w_new.mean() * 1.5 < w_old.mean()
+    assert capi.plan_locality_order(4, rp[:5] * 0, col[:0], 8, 512) is None  # fewer cells than needed
+
+
+@pytest.mark.parametrize("per_edge_g", [False, True])
+def test_relabelled_stamped_plan_emulates_exactly(capi, per_edge_g):
+    """The planner relabels a wide-window grid network; the emulated currents,
+    reported in the caller's order, match the direct CSR computation."""
+    n = 3600
+    rp, col = capi.gen_grid_gaussian(60, 60, 6.0, 11.0, 4)
+    rp, col = np.asarray(rp), np.asarray(col)
+    g = np.random.default_rng(3).uniform(0.02, 0.06, len(col)).astype(np.float32) if per_edge_g else None
+    info = check(capi, n, rp, col, g=g, threads=512)
+    assert info["stamped"] == 1 and info["relabelled"]
+
+
+def test_random_graph_keeps_caller_order(capi):
+    """No spatial structure: the relabelled plan would not narrow the windows,
+    so the plan keeps the caller's cell order."""
+    rp, col = capi.gen_uniform(3000, 0.02, 1)
+    info = check(capi, 3000, rp, col, threads=512)
+    assert info["stamped"] == 1 and not info["relabelled"]
