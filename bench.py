@@ -250,13 +250,13 @@ def run_gpu(args, world, rank, local):
 
     # ---- e2e through the C ABI from host buffers
     host_state = torch.from_numpy(st).pin_memory().numpy()
-    out_state = np.empty_like(st)
+    out_state = torch.empty(st.shape, dtype=torch.float32).pin_memory().numpy()
     dist_barrier(world)
     t0 = time.perf_counter()
     for _ in range(args.steps):
         sim.set_state(host_state)
         sim.run_with_callback(STEPS_PER_ITER, TRACE_EVERY, ig.TRACE_AXON, on_row)
-        out_state[:] = sim.get_state()
+        sim.get_state(out=out_state)
     e2e_s = dist_max(time.perf_counter() - t0, world)
     rows_per_iter = STEPS_PER_ITER // TRACE_EVERY
     h2d = 19 * 4 * n

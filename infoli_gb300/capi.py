@@ -487,8 +487,12 @@ class Simulation:
         cb = TRACE_CB(_cb)
         _check(self._L.infoli_sim_run(self._h, int(n_steps), int(trace_every), int(what), cb, None))
 
-    def get_state(self) -> np.ndarray:
-        out = np.zeros((NSTATE, self.n), dtype=np.float32)
+    def get_state(self, out=None) -> np.ndarray:
+        """The 19 state arrays [19, n]; written into `out` (float32, C-contiguous,
+        e.g. a pinned buffer) when given."""
+        if out is None:
+            out = np.empty((NSTATE, self.n), dtype=np.float32)
+        assert out.dtype == np.float32 and out.flags.c_contiguous and out.size == NSTATE * self.n
         _check(self._L.infoli_sim_get_state(self._h, _p(out)))
         return out
 

@@ -109,6 +109,7 @@ struct infoli_sim {
   float* d_vd[2] = {nullptr, nullptr};
   float* d_st = nullptr;
   double* d_ca = nullptr;
+  float* d_io = nullptr;  // the C ABI's 19 x n state layout, staged on the device
   // stimulus
   int stim_kind = STIM_PULSE;
   int stim_start = 20000, stim_end = 20499;
@@ -145,7 +146,7 @@ void release(infoli_sim* s) {
                    s->d_edge_g, s->d_vd[0], s->d_vd[1],  s->d_st,         s->d_ca,
                    s->d_cell_amp, s->d_cell_onset, s->d_bar, s->d_err, s->d_trace[0], s->d_trace[1],
                    s->d_prof, s->d_probes, s->d_vll[0], s->d_vll[1], s->d_gdesc, s->d_stim_table,
-                   s->d_gcol, s->d_perm};
+                   s->d_gcol, s->d_perm, s->d_io};
   if (s->stream) {
     for (void* p : dptrs)
       if (p) cudaFreeAsync(p, s->stream);
@@ -165,29 +166,64 @@ const int kFieldOfState[INFOLI_NSTATE] = {
     -1 /*V_dend -> vd*/, F_R, F_S, F_Q, -2 /*Ca2Plus -> ca*/, F_ICAH, F_GCAL, F_VS, F_M, F_H, F_N, F_P,
     F_XS, F_K, F_L, F_VA, F_MA, F_HA, F_XA};
 
+struct StateMap {
+  int field[INFOLI_NSTATE];
+};
+
+// ABI layout (19 x n floats, reference order) <-> device layout (F_COUNT x
+// n_pad floats, FP64 Ca2+, V_dend in both halves of its double buffer).
+// One thread per (array, cell); padding cells stay as they are.
+__global__ void state_scatter_kernel(const float* __restrict__ in, int n, long long np, StateMap m, float* st,
+                                     double* ca, float* vd0, float* vd1) {
+  const long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= (long long)INFOLI_NSTATE * n) return;
+  const int k = (int)(i / n), c = (int)(i - (long long)k * n);
+  const float v = in[i];
+  const int f = m.field[k];
+  if (f == -1) {
+    vd0[c] = v;
+    vd1[c] = v;
+  } else if (f == -2) {
+    ca[c] = (double)v;
+  } else {
+    st[(long long)f * np + c] = v;
+  }
+}
+
+__global__ void state_gather_kernel(float* __restrict__ out, int n, long long np, StateMap m, const float* st,
+                                    const double* ca, const float* vd) {
+  const long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= (long long)INFOLI_NSTATE * n) return;
+  const int k = (int)(i / n), c = (int)(i - (long long)k * n);
+  const int f = m.field[k];
+  out[i] = f == -1 ? vd[c] : f == -2 ? (float)ca[c] : st[(long long)f * np + c];
+}
+
+StateMap state_map() {
+  StateMap m;
+  for (int k = 0; k < INFOLI_NSTATE; ++k) m.field[k] = kFieldOfState[k];
+  return m;
+}
+
+int state_io_buffer(infoli_sim* s) {
+  if (s->d_io) return INFOLI_OK;
+  return pool_alloc(&s->d_io, (size_t)INFOLI_NSTATE * s->n * sizeof(float), s->device, s->stream) == cudaSuccess
+             ? INFOLI_OK
+             : infoli__fail(INFOLI_ERR_NOMEM, "state staging buffer: device allocation failed");
+}
+
+// One host->device copy of the caller's 19 x n array (a direct DMA when the
+// caller's buffer is pinned), then the scatter on the device.  Returns after
+// the copy has completed, so the caller may reuse its buffer.
 int upload_state(infoli_sim* s, const float* state /*19 x n*/) {
   const int n = s->n;
-  const size_t np = (size_t)s->n_pad;
-  std::vector<float> st((size_t)F_COUNT * np, 0.0f);
-  std::vector<double> ca(np, 0.0);
-  std::vector<float> vd(np, 0.0f);
-  for (int k = 0; k < INFOLI_NSTATE; ++k) {
-    const float* src = state + (size_t)k * n;
-    const int f = kFieldOfState[k];
-    if (f == -1)
-      std::copy(src, src + n, vd.begin());
-    else if (f == -2)
-      for (int c = 0; c < n; ++c) ca[c] = (double)src[c];
-    else
-      std::copy(src, src + n, st.begin() + (size_t)f * np);
-  }
-  // pageable sources: each call returns once its data is staged, so the
-  // local vectors may go out of scope
-  CK(cudaMemcpyAsync(s->d_st, st.data(), st.size() * sizeof(float), cudaMemcpyHostToDevice, s->stream));
-  CK(cudaMemcpyAsync(s->d_ca, ca.data(), ca.size() * sizeof(double), cudaMemcpyHostToDevice, s->stream));
-  CK(cudaMemcpyAsync(s->d_vd[s->step & 1], vd.data(), np * sizeof(float), cudaMemcpyHostToDevice, s->stream));
-  CK(cudaMemcpyAsync(s->d_vd[(s->step + 1) & 1], vd.data(), np * sizeof(float), cudaMemcpyHostToDevice,
-                     s->stream));
+  const long long total = (long long)INFOLI_NSTATE * n;
+  if (int rc = state_io_buffer(s)) return rc;
+  CK(cudaMemcpyAsync(s->d_io, state, (size_t)total * sizeof(float), cudaMemcpyHostToDevice, s->stream));
+  state_scatter_kernel<<<(unsigned)((total + 255) / 256), 256, 0, s->stream>>>(
+      s->d_io, n, (long long)s->n_pad, state_map(), s->d_st, s->d_ca, s->d_vd[s->step & 1],
+      s->d_vd[(s->step + 1) & 1]);
+  CK(cudaGetLastError());
   CK(cudaStreamSynchronize(s->stream));
   return INFOLI_OK;
 }
@@ -721,23 +757,15 @@ int infoli_sim_get_state(infoli_sim* s, float* out) {
   if (!s || !out) return infoli__fail(INFOLI_ERR_ARG, "get_state: bad argument");
   CK(cudaSetDevice(s->device));
   CK(cudaStreamSynchronize(s->stream));
+  // gather on the device into the ABI layout, then one device->host copy
   const int n = s->n;
-  const size_t np = (size_t)s->n_pad;
-  std::vector<float> st((size_t)F_COUNT * np), vd(np);
-  std::vector<double> ca(np);
-  CK(cudaMemcpy(st.data(), s->d_st, st.size() * sizeof(float), cudaMemcpyDeviceToHost));
-  CK(cudaMemcpy(ca.data(), s->d_ca, ca.size() * sizeof(double), cudaMemcpyDeviceToHost));
-  CK(cudaMemcpy(vd.data(), s->d_vd[s->step & 1], np * sizeof(float), cudaMemcpyDeviceToHost));
-  for (int k = 0; k < INFOLI_NSTATE; ++k) {
-    float* dst = out + (size_t)k * n;
-    const int f = kFieldOfState[k];
-    if (f == -1)
-      std::copy(vd.begin(), vd.begin() + n, dst);
-    else if (f == -2)
-      for (int c = 0; c < n; ++c) dst[c] = (float)ca[c];
-    else
-      std::copy(st.begin() + (size_t)f * np, st.begin() + (size_t)f * np + n, dst);
-  }
+  const long long total = (long long)INFOLI_NSTATE * n;
+  if (int rc = state_io_buffer(s)) return rc;
+  state_gather_kernel<<<(unsigned)((total + 255) / 256), 256, 0, s->stream>>>(
+      s->d_io, n, (long long)s->n_pad, state_map(), s->d_st, s->d_ca, s->d_vd[s->step & 1]);
+  CK(cudaGetLastError());
+  CK(cudaMemcpyAsync(out, s->d_io, (size_t)total * sizeof(float), cudaMemcpyDeviceToHost, s->stream));
+  CK(cudaStreamSynchronize(s->stream));
   return INFOLI_OK;
 }
 
