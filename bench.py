@@ -156,6 +156,11 @@ def dist_barrier(world):
         dist.barrier()
 
 
+def workload_name():
+    """The network both arms run (the same string in both JSON lines)."""
+    return f"grid {ROWS}x{COLS} gaussian sigma={SIGMA} radius={RADIUS} g=0.04 seed=1"
+
+
 def cpu_port_rate(conf, n, rp, col, st, steps, threads):
     """Oracle restatement of the reference OpenMP loop on the host cores: cell-steps/s."""
     from oracle import oracle as O
@@ -190,8 +195,9 @@ def run_reference(args, world, rank):
         "n_gpus": args.gpus, "steps": args.steps, "warmup": args.warmup,
         "ms_per_step": 1e3 * total / args.steps, "higher_is_better": True, "scaling": "weak",
         "vs_baseline": None, "dtype": "f32", "data": "synthetic",
-        "config": {"workload": f"grid {ROWS}x{COLS} gaussian sigma={SIGMA} radius={RADIUS}, {len(col)} edges",
-                   "cells": n, "edges": int(len(col)), "timesteps_per_step": sample},
+        "config": {"workload": workload_name(), "cells": n, "edges": int(len(col)),
+                   "mean_degree": float(len(col) / n), "timesteps_per_step": sample,
+                   "trace": f"V_axon every {TRACE_EVERY} timesteps"},
         "cpu_baseline": {"value": value, "unit": "cell-steps/s", "cores": threads, "kind": "port",
                          "sample": f"{sample} timesteps of the workload per bench step, OpenMP over cells"},
         "e2e": {"value": value, "unit": "cell-steps/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
@@ -292,10 +298,9 @@ def run_gpu(args, world, rank, local):
             "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
             "data": "synthetic",
             "config": {
-                "workload": f"grid {ROWS}x{COLS} gaussian sigma={SIGMA} radius={RADIUS} g=0.04, "
-                            f"{STEPS_PER_ITER} timesteps per step, V_axon trace every {TRACE_EVERY}",
-                "cells": n, "edges": int(len(col)), "mean_degree": float(len(col) / n),
-                "timesteps_per_step": STEPS_PER_ITER, "l2": "flushed between timed steps (256 MB memset)",
+                "workload": workload_name(), "cells": n, "edges": int(len(col)), "mean_degree": float(len(col) / n),
+                "timesteps_per_step": STEPS_PER_ITER, "trace": f"V_axon every {TRACE_EVERY} timesteps",
+                "l2": "flushed between timed steps (256 MB memset)",
                 "parallelism": f"replicas x{world}" if world > 1 else "single GPU",
                 "plan": plan,
             },
