@@ -156,6 +156,24 @@ def dist_barrier(world):
         dist.barrier()
 
 
+ACC_STEPS = 2000  # window of the accuracy criterion: max |dV_soma| <= 1e-3 mV over the first 2000 steps
+ACC_TOL_MV = 1e-3
+
+
+def soma_error_vs_fp64(conf, n, rp, col, st, gpu_soma, g_uniform, threads, final_only=False):
+    """max |V_soma(GPU) - V_soma(FP64 oracle)| in mV over ACC_STEPS steps from the
+    initial state `st` (every step, or only the state after the last step)."""
+    import numpy as np
+    from oracle import oracle as O
+
+    s64 = np.ascontiguousarray(st, dtype=np.float64)
+    ref = O.run(n, np.asarray(conf[:23], dtype=np.float64), s64, rp, col, g_uniform=g_uniform, nsteps=ACC_STEPS,
+                trace_every=0 if final_only else 1, traces=() if final_only else ("soma",), nthreads=threads,
+                fp64=True)
+    want = s64[O.S["V_soma"]] if final_only else ref["soma"]
+    return float(np.max(np.abs(np.asarray(gpu_soma, dtype=np.float64) - want)))
+
+
 def workload_name():
     """The network both arms run (the same string in both JSON lines)."""
     return f"grid {ROWS}x{COLS} gaussian sigma={SIGMA} radius={RADIUS} g=0.04 seed=1"
@@ -273,6 +291,9 @@ def run_gpu(args, world, rank, local):
     sim.run(STEPS_PER_ITER)
     prof = sim.get_profile()
     sim.set_profiling(False)
+    # ---- accuracy: the same initial state, ACC_STEPS steps, V_soma every step
+    sim.set_state(st)
+    gpu_soma = sim.run(ACC_STEPS, 1, ig.TRACE_SOMA)["soma"]
     sim.close()
 
     cell_steps = n * STEPS_PER_ITER * args.steps * world
@@ -292,6 +313,7 @@ def run_gpu(args, world, rank, local):
         clocks = clk.summary()
         threads = os.cpu_count() or 1
         cpu_rate, cpu_dt = cpu_port_rate(conf, n, rp, col, st, CPU_SAMPLE_STEPS, threads)
+        acc = soma_error_vs_fp64(conf, n, rp, col, st, gpu_soma, conf[1], threads)
         result = {
             "metric": "cell-steps/s", "value": value, "unit": "cell-steps/s", "n_gpus": world,
             "steps": args.steps, "warmup": args.warmup, "ms_per_step": total_dev_ms / args.steps,
@@ -316,6 +338,8 @@ def run_gpu(args, world, rank, local):
                                  f"DRAM read+write of one launch of this workload (profiles/): the "
                                  f"topology and V_dend windows stay on chip, the step is latency-bound"},
             "phase_ns_per_timestep": prof["max"],
+            "accuracy": {"max_abs_dV_soma_mV": acc, "steps": ACC_STEPS, "vs": "FP64 oracle (oracle/, same "
+                         "initial state and topology)", "tolerance_mV": ACC_TOL_MV, "pass": acc <= ACC_TOL_MV},
             "clocks": clocks,
             "cpu_baseline": {"value": cpu_rate, "unit": "cell-steps/s", "cores": threads, "kind": "port",
                              "sample": f"{CPU_SAMPLE_STEPS} timesteps of the same workload ({cpu_dt:.1f} s)"},
@@ -443,9 +467,25 @@ def run_gpu_batched(args, world, rank, local):
             plain_s += sim.last_run_stats()[0] * 1e-3
     plain_rate = len(nets) / (plain_s * (len(nets) / len(picks)) * (BATCH_TIMESTEPS / BATCH_STEP))
 
+    # accuracy: the three smallest networks as a batch of their own, ACC_STEPS
+    # steps, final V_soma against the FP64 oracle
+    acc_ids = [int(i) for i in np.argsort(meta["sizes"])[:3]]
+    acc_nets = [nets[i] for i in acc_ids]
+    acc_st = np.concatenate([st[:, off[i]:off[i + 1]] for i in acc_ids], axis=1)
+    with ig.Batch(conf, acc_nets, init_state=acc_st, kahan=True, device=local) as ab:
+        ab.run(ACC_STEPS)
+        acc_out = ab.get_state()
+        acc_soma = [ab.net_state(acc_out, k)[7] for k in range(len(acc_ids))]
+
     result = None
     if rank == 0:
         threads = os.cpu_count() or 1
+        acc = 0.0
+        for k, i in enumerate(acc_ids):
+            n_i, bits_i, g_i = nets[i]
+            rp_i, col_i = ig.bitmask_to_csr(n_i, bits_i)
+            acc = max(acc, soma_error_vs_fp64(conf, n_i, rp_i, col_i, st[:, off[i]:off[i + 1]], acc_soma[k], g_i,
+                                              threads, final_only=True))
         cpu_rate, cpu_t, cpu_picks = cpu_batched_rate(conf, nets, st, meta, threads)
         # algorithmic bytes of one launch: the bitmask rows once per timestep
         # (networks whose rows stay in shared memory are still counted) and 132 B
@@ -466,6 +506,9 @@ def run_gpu_batched(args, world, rank, local):
             "cell_steps_per_s": int(meta["sizes"].sum()) * BATCH_STEP * args.steps * world / (total_dev_ms * 1e-3),
             "edge_evals_per_s": edges * BATCH_STEP * args.steps * world / (total_dev_ms * 1e-3),
             "finite_fraction": finite,
+            "accuracy": {"max_abs_dV_soma_mV": acc, "steps": ACC_STEPS, "networks": acc_ids,
+                         "vs": "FP64 oracle, V_soma after the last step (the batch's three smallest networks run "
+                               "as a batch of their own)", "tolerance_mV": ACC_TOL_MV, "pass": acc <= ACC_TOL_MV},
             "sequential_plain": {"value": plain_rate, "unit": "sims/s", "sample": f"networks {picks}, "
                                  f"{BATCH_STEP} timesteps each through infoli_sim (Kahan), device time, "
                                  f"extrapolated to {len(nets)} networks x {BATCH_TIMESTEPS} timesteps"},
