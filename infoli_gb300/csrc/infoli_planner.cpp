@@ -598,13 +598,16 @@ bool make_plan_base(const PlanInput& in, Plan* out, std::string* err) {
       *err = "make_plan: row_ptr not monotone";
       return false;
     }
+  int64_t bad = E;  // first edge with an out-of-range sender id
+#pragma omp parallel for schedule(static) reduction(min : bad)
   for (int64_t e = 0; e < E; ++e)
-    if (in.col[e] < 0 || in.col[e] >= n) {
-      char b[128];
-      snprintf(b, sizeof b, "make_plan: sender id %d out of range at edge %lld", in.col[e], (long long)e);
-      *err = b;
-      return false;
-    }
+    if (in.col[e] < 0 || in.col[e] >= n) bad = std::min(bad, e);
+  if (bad < E) {
+    char b[128];
+    snprintf(b, sizeof b, "make_plan: sender id %d out of range at edge %lld", in.col[bad], (long long)bad);
+    *err = b;
+    return false;
+  }
   if (E > INT32_MAX) {
     *err = "make_plan: more than 2^31-1 edges";
     return false;
@@ -612,6 +615,13 @@ bool make_plan_base(const PlanInput& in, Plan* out, std::string* err) {
   if (in.sync_mode == kSyncGather) return make_gather_plan(in, out, err);
   if (in.sync_mode == kSyncTiledGather) return make_tgather_plan(in, out, err);
   if (in.sync_mode == kSyncBits) return make_bits_plan(in, out, err);
+  // dense rows with one conductance whose edges cannot stay resident in shared
+  // memory (2 bytes per edge per CTA): no stamped plan is possible, and auto
+  // mode would pick the bitmask plan after building the tile plan; build it
+  // directly
+  if (in.sync_mode == kSyncAuto && !in.g && E * kBitsMinDensityInv >= (int64_t)n * (int64_t)n &&
+      (E / std::max(1, in.grid_max)) * (int64_t)sizeof(uint16_t) > (int64_t)in.smem_budget)
+    return make_bits_plan(in, out, err);
   const int threads = in.threads;
   const int nwarps = threads / 32;
   const int n_pad = pad_cells(n);
