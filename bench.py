@@ -626,11 +626,12 @@ def run_gpu_serving(args, world, rank, local):
     # sequential plain runs: each request alone through infoli_sim (create +
     # run + state read back, the whole GPU), then a first-in-first-out
     # schedule with the same arrival times
-    service = []
+    service, plain_create = [], []
     for r in reqs:
         ts = time.perf_counter()
         with ig.Simulation(r["n"], conf, r["row_ptr"], r["col"], g_uniform=0.04, init_state=r["init_state"],
                            kahan=True, device=local) as sim:
+            plain_create.append(time.perf_counter() - ts)
             sim.run(r["n_steps"])
             sim.get_state()
         service.append(time.perf_counter() - ts)
@@ -652,7 +653,12 @@ def run_gpu_serving(args, world, rank, local):
                                    f"bench step), sizes log-uniform 500-50000 cells, durations U(100,2000) ms, "
                                    f"density U(0.01,0.30), g=0.04, admitted by HBM budget (80% of free memory)",
                        "requests": count, "cells": [r["n"] for r in reqs], "steps": [r["n_steps"] for r in reqs],
-                       "edges": [int(len(r["col"])) for r in reqs], "timing": "host wall clock from the first "
+                       "edges": [int(len(r["col"])) for r in reqs],
+                       "scheduling": "admission first in first out by HBM budget (up to 64 admitted); prepared "
+                                     "requests launch shortest estimated work (edges x steps) first, any "
+                                     "submitted more than 10 s ago ahead of them; SM share one CTA per 32768 "
+                                     "edge evaluations per step",
+                       "timing": "host wall clock from the first "
                        "arrival to the last result (serving is end to end)", "l2": "inputs larger than L2"},
             "latency_s": {"p50": float(np.percentile(lat, 50)), "p99": float(np.percentile(lat, 99)),
                           "max": float(lat.max())},
@@ -666,9 +672,12 @@ def run_gpu_serving(args, world, rank, local):
             "e2e": {"value": served, "unit": "sims/s", "h2d_bytes_per_step": int(in_bytes / count),
                     "d2h_bytes_per_step": int(sum(19 * 4 * r["n"] for r in reqs) / count)},
             "grid_per_request": [i["grid"] for i in infos],
-            "prepare_s_per_request": [round(i["prepared_s"] - i["admit_s"], 3) for i in infos],
+            "prep_queue_s_per_request": [round(i["prep_start_s"] - i["admit_s"], 3) for i in infos],
+            "prepare_s_per_request": [round(i["prepared_s"] - i["prep_start_s"], 3) for i in infos],
+            "launch_wait_s_per_request": [round(i["start_s"] - i["prepared_s"], 3) for i in infos],
             "run_s_per_request": [round(i["done_s"] - i["start_s"], 3) for i in infos],
             "plain_service_s_per_request": [round(x, 3) for x in service],
+            "plain_create_s_per_request": [round(x, 3) for x in plain_create],
             "gpu_launches": int(sum((r["n_steps"] + 8191) // 8192 for r in reqs)),
             "clocks": clk.summary(),
         }

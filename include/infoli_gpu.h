@@ -350,11 +350,14 @@ typedef struct {
   const float* params;   /* [INFOLI_NPARAM] shared by all requests */
   int device;
   int64_t hbm_budget;    /* device bytes admitted requests may hold; 0 = 80% of free memory */
-  int max_active;        /* requests admitted at once (preparing or running); 0 = 16 */
+  int max_active;        /* requests admitted at once (preparing or running); 0 = 64 */
   int64_t work_per_cta;  /* edge evaluations per step per CTA when sizing a request's SM share; 0 = 32768 */
   int backfill_ms;       /* later requests may pass a head request that does not fit yet for this long; 0 = 1000 */
   int prep_threads;      /* host threads building plans; 0 = 4 */
   int flags;             /* INFOLI_F_KAHAN for every request */
+  int age_ms;            /* prepared requests launch shortest estimated work (edges x steps) first;
+                            one submitted this long ago goes ahead of them (oldest first); 0 = 10000,
+                            < 0 = arrival order */
 } infoli_server_desc;
 
 typedef struct {
@@ -380,6 +383,7 @@ typedef struct {
    * upload done, launched, finished */
   double submit_s, admit_s, prepared_s, start_s, done_s;
   int status;                 /* INFOLI_OK or the request's error */
+  double prep_start_s;        /* a preparation thread took it (admit_s .. prep_start_s: queued for one) */
 } infoli_request_info;
 
 int infoli_server_create(const infoli_server_desc* desc, infoli_server** out);

@@ -98,6 +98,7 @@ class ServerDesc(C.Structure):
         ("backfill_ms", C.c_int),
         ("prep_threads", C.c_int),
         ("flags", C.c_int),
+        ("age_ms", C.c_int),
     ]
 
 
@@ -131,6 +132,7 @@ class RequestInfo(C.Structure):
         ("start_s", C.c_double),
         ("done_s", C.c_double),
         ("status", C.c_int),
+        ("prep_start_s", C.c_double),
     ]
 
 

@@ -99,12 +99,21 @@ std::vector<TileSpan> make_tiles(const std::vector<int>& u, int cap, int n_pad) 
 void pack_groups(Plan& P, const SmemLayout& L, const PlanInput& in, const std::vector<std::vector<int>>& win,
                  int dup_words) {
   const bool edge_g = in.g != nullptr;
-  std::vector<int2_t> gdesc;
-  std::vector<uint16_t> pe;
-  std::vector<float> pg;
+  // CTAs are packed in parallel into local tables, then concatenated
+  struct Local {
+    std::vector<int2_t> gdesc;
+    std::vector<uint16_t> pe;
+    std::vector<float> pg;
+  };
+  const int ctas = (int)P.cta.size();
+  std::vector<Local> loc(ctas);
   int max_slots = 1;
-  for (size_t b = 0; b < P.cta.size(); ++b) {
+#pragma omp parallel for schedule(dynamic, 1) reduction(max : max_slots)
+  for (int b = 0; b < ctas; ++b) {
     CtaWork& w = P.cta[b];
+    std::vector<int2_t>& gdesc = loc[b].gdesc;
+    std::vector<uint16_t>& pe = loc[b].pe;
+    std::vector<float>& pg = loc[b].pg;
     const std::vector<int>& u = win[b];
     struct LaneChunk {
       int recv, slot;
@@ -137,7 +146,6 @@ void pack_groups(Plan& P, const SmemLayout& L, const PlanInput& in, const std::v
     w.n_slots = slot;
     max_slots = std::max(max_slots, slot + 1);
     const int ng = (int)(lc.size() + 31) / 32;
-    w.group_begin = (int)(gdesc.size() / 32);
     w.n_groups = ng;
     for (int g = 0; g < ng; ++g) {
       // the 32 chunks of this group (dummies past the end)
@@ -252,6 +260,18 @@ void pack_groups(Plan& P, const SmemLayout& L, const PlanInput& in, const std::v
           if (edge_g) pg[at] = cell[l * kLaneEdges + k].second;
         }
     }
+  }
+  std::vector<int2_t> gdesc;
+  std::vector<uint16_t> pe;
+  std::vector<float> pg;
+  for (int b = 0; b < ctas; ++b) {
+    P.cta[b].group_begin = (int)(gdesc.size() / 32);
+    gdesc.insert(gdesc.end(), loc[b].gdesc.begin(), loc[b].gdesc.end());
+    pe.insert(pe.end(), loc[b].pe.begin(), loc[b].pe.end());
+    pg.insert(pg.end(), loc[b].pg.begin(), loc[b].pg.end());
+    Local().gdesc.swap(loc[b].gdesc);
+    Local().pe.swap(loc[b].pe);
+    Local().pg.swap(loc[b].pg);
   }
   P.gdesc.swap(gdesc);
   P.edges.swap(pe);

@@ -17,7 +17,10 @@
 //               running simulations (the grids of all running simulations
 //               never exceed the SM count, so every persistent grid is
 //               co-resident and none waits on another); its work overlaps
-//               the others' on the device;
+//               the others' on the device.  Among prepared requests, those
+//               submitted longer ago than the age limit go first (oldest
+//               first), then the shortest estimated work (edges x steps);
+//               a negative age limit keeps arrival order;
 //   done     -> final state copied to the host, device memory released; the
 //               record waits for infoli_server_wait.
 // A request's result does not depend on what runs beside it: its plan and
@@ -56,8 +59,9 @@ struct Request {
   int flags = 0;
   // scheduling
   int grid = 0;
+  double work = 0;  // estimated edge evaluations (plus a per-cell share) over the whole run
   int64_t est_bytes = 0, dev_bytes = 0, admit_bytes = 0;
-  double submit_s = 0, admit_s = 0, prepared_s = 0, start_s = 0, done_s = 0;
+  double submit_s = 0, admit_s = 0, prep_start_s = 0, prepared_s = 0, start_s = 0, done_s = 0;
   int phase = 0;  // 0 queued, 1 admitted (preparing), 2 prepared, 3 running, 4 done
   int status = INFOLI_OK;
   char err[256] = {0};
@@ -69,9 +73,10 @@ struct Request {
 
 struct infoli_server {
   std::vector<float> params;
-  int device = 0, nsm = 0, max_active = 16, flags = 0;
+  int device = 0, nsm = 0, max_active = 64, flags = 0;
   int64_t budget = 0, work_per_cta = 0;
   double backfill_s = 1.0;
+  double age_s = 10.0;  // < 0: launch in arrival order
   Clock::time_point t0;
   std::mutex m;
   std::condition_variable cv_sched, cv_prep, cv_done;
@@ -128,6 +133,7 @@ void prep_loop(infoli_server* sv) {
     Request* r = sv->to_prep.front();
     sv->to_prep.pop_front();
     ++sv->preparing;
+    r->prep_start_s = sv->now();
     lk.unlock();
     InfoliRange nvtx_range("infoli_server_prepare");
     infoli_sim_desc d;
@@ -229,7 +235,16 @@ void sched_loop(infoli_server* sv) {
       if (it == sv->queue.begin() && t - r->submit_s > sv->backfill_s) break;  // the head waits no longer
       ++it;
     }
-    // launch prepared simulations whose grids fit beside the running ones
+    // launch prepared simulations whose grids fit beside the running ones:
+    // requests submitted more than age_s ago first (oldest first), then the
+    // shortest estimated work first
+    if (sv->age_s >= 0) {
+      std::stable_sort(sv->ready.begin(), sv->ready.end(), [&](const Request* a, const Request* b) {
+        const bool oa = t - a->submit_s > sv->age_s, ob = t - b->submit_s > sv->age_s;
+        if (oa != ob) return oa;
+        return oa ? a->submit_s < b->submit_s : a->work < b->work;
+      });
+    }
     for (size_t i = 0; i < sv->ready.size();) {
       Request* r = sv->ready[i];
       if (sv->grid_in_use + r->grid > sv->nsm) {
@@ -276,7 +291,8 @@ extern "C" int infoli_server_create(const infoli_server_desc* d, infoli_server**
   sv->params.assign(d->params, d->params + INFOLI_NPARAM);
   sv->device = d->device;
   sv->flags = d->flags;
-  sv->max_active = d->max_active > 0 ? d->max_active : 16;
+  sv->max_active = d->max_active > 0 ? d->max_active : 64;
+  sv->age_s = d->age_ms > 0 ? d->age_ms * 1e-3 : d->age_ms < 0 ? -1.0 : 10.0;
   sv->work_per_cta = d->work_per_cta > 0 ? d->work_per_cta : (int64_t)1 << 15;
   sv->backfill_s = d->backfill_ms > 0 ? d->backfill_ms * 1e-3 : 1.0;
   cudaSetDevice(sv->device);
@@ -321,6 +337,8 @@ extern "C" int infoli_server_submit(infoli_server* sv, const infoli_request_desc
   r->est_bytes = estimate_bytes(n, edges, q->g != nullptr);
   r->admit_bytes = r->est_bytes;
   r->grid = grid_for(sv, n, edges);
+  // the cell update costs about as much as 100 edge evaluations per cell-step
+  r->work = ((double)edges + 100.0 * (double)n) * (double)q->n_steps;
   std::lock_guard<std::mutex> lk(sv->m);
   if (r->est_bytes > sv->budget) {
     const long long need = (long long)r->est_bytes, have = (long long)sv->budget;
@@ -366,6 +384,7 @@ extern "C" int infoli_server_wait(infoli_server* sv, int64_t id, float* out_stat
     info->submit_s = r->submit_s;
     info->admit_s = r->admit_s;
     info->prepared_s = r->prepared_s;
+    info->prep_start_s = r->prep_start_s;
     info->start_s = r->start_s;
     info->done_s = r->done_s;
     info->status = r->status;
