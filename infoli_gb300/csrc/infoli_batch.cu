@@ -79,6 +79,12 @@ __device__ __forceinline__ unsigned cluster_rank() {
 
 // Store a float into the shared memory of CTA `peer` of this cluster at the
 // address that `local` has in this CTA.
+// The V_dend buffers hold V * kVScale (kVScale^2 = log2(e) / 100), so a
+// coupling term's exponent is -(dV')^2 with dV' = kVScale dV: one multiply
+// less per edge; the sums are scaled back once per receiver.
+constexpr float kVScale = 0.12011224087864497f;
+constexpr float kInvVScale = 8.325546111576978f;
+
 __device__ __forceinline__ void st_peer(float* local, unsigned peer, float v) {
   const unsigned la = smem_u32(local);
   unsigned ra;
@@ -131,8 +137,8 @@ __device__ __forceinline__ float couple_warp(bool own, uint32_t wsm, uint32_t ws
       const int c = __clz(x);  // 32 once x is used up
       const bool live = x != 0u;
       x &= __funnelshift_rc(0x7fffffffu, 0u, (unsigned)c);
-      const float V = vc - ld_shared_f32(vcol + 4u * (uint32_t)c);
-      const float f = fmaf(0.8f, ex2_approx((V * V) * kNegLog2eOver100), 0.2f);
+      const float V = vc - ld_shared_f32(vcol + 4u * (uint32_t)c);  // scaled by kVScale
+      const float f = fmaf(0.8f, ex2_approx(-(V * V)), 0.2f);
       if (live) col = fmaf(f, V, col);
     }
     if (KAHAN) {
@@ -195,9 +201,9 @@ __global__ void __launch_bounds__(BLOCK, 1) batch_kernel(const __grid_constant__
   }
   cluster_sync_all();  // every CTA of the cluster is running before peers write into it
   if (own) {
-    vbuf[r] = v.Vd;
+    vbuf[r] = v.Vd * kVScale;
     for (int p = 0; p < w.ncta; ++p)
-      if (w.rank0 + p != (int)me) st_peer(vbuf + r, (unsigned)(w.rank0 + p), v.Vd);
+      if (w.rank0 + p != (int)me) st_peer(vbuf + r, (unsigned)(w.rank0 + p), v.Vd * kVScale);
   }
   cluster_sync_all();
 
@@ -210,21 +216,23 @@ __global__ void __launch_bounds__(BLOCK, 1) batch_kernel(const __grid_constant__
     float sum = 0.0f;
     if (w.net >= 0 && (tid & ~31) < w.ncell) {
       const uint32_t vbase = smem_u32(vcur);
+      const float vcs = v.Vd * kVScale;
       sum = w.resident ? couple_warp<KAHAN, true>(own, smem_u32(sbits + tid), 4u * BLOCK, nullptr, 0u, w.wpr, vbase,
-                                                  v.Vd)
+                                                  vcs)
                        : couple_warp<KAHAN, false>(own, 0u, 0u, a.bits + w.bits_base + r, (uint32_t)w.n, w.wpr,
-                                                   vbase, v.Vd);
+                                                   vbase, vcs);
     }
     if (own) {
-      const float ic = sum * w.g;
+      const float ic = sum * (w.g * kInvVScale);
       const float iapp = (step >= a.pulse_start && step < a.pulse_end) ? a.pulse_amp : 0.0f;
       // ---- fused compartment update
       Currents cur;
       run_units(a.P, 0xffu, v, gs, cur);
       voltage_step(a.P, vk, v, cur, ic, iapp);
-      vnxt[r] = v.Vd;
+      const float vds = v.Vd * kVScale;
+      vnxt[r] = vds;
       for (int p = 0; p < w.ncta; ++p)
-        if (w.rank0 + p != (int)me) st_peer(vnxt + r, (unsigned)(w.rank0 + p), v.Vd);
+        if (w.rank0 + p != (int)me) st_peer(vnxt + r, (unsigned)(w.rank0 + p), vds);
     }
     if (w.cl_sync)
       cluster_sync_all();
