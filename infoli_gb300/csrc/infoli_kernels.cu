@@ -458,6 +458,10 @@ __global__ void __launch_bounds__(BLOCK, 1) step_kernel(const __grid_constant__ 
     }
   }
 
+  // stamped plans read each receiver's partial slots four at a time: the gaps
+  // between receivers' slot blocks must hold zeros (nothing writes them)
+  if (LL)
+    for (int i = tid; i < shp.max_slots; i += blockDim.x) part[i] = 0.0f;
   if (tid == 0) {
     mbar_init(&mbar[0], 1);
     mbar_init(&mbar[1], 1);
@@ -607,6 +611,19 @@ __global__ void __launch_bounds__(BLOCK, 1) step_kernel(const __grid_constant__ 
           s = tt;
         }
         ic = s;
+      } else if (LL) {
+        // stamped plans: a receiver's slots start on a 16-byte boundary and the
+        // gaps after them hold zeros, so read them as float4 (slot order kept)
+        ic = 0.0f;
+        const float4* p4 = reinterpret_cast<const float4*>(part + slots.x);
+        const int nq = (slots.y + 3) >> 2;
+        for (int q = 0; q < nq; ++q) {
+          const float4 p = p4[q];
+          ic += p.x;
+          ic += p.y;
+          ic += p.z;
+          ic += p.w;
+        }
       } else {
         // in slot (= sender) order; four loads in flight at a time
         ic = 0.0f;

@@ -127,6 +127,9 @@ void pack_groups(Plan& P, const SmemLayout& L, const PlanInput& in, const std::v
       for (int64_t e = in.row_ptr[c]; e < in.row_ptr[c + 1]; ++e) snd.push_back({in.col[e], edge_g ? in.g[e] : 0.0f});
       std::stable_sort(snd.begin(), snd.end(),
                        [](const std::pair<int, float>& x, const std::pair<int, float>& y) { return x.first < y.first; });
+      // each receiver's partial slots start on a 4-slot (16-byte) boundary; the
+      // gaps are zeroed once per launch, so the update can read them 4 at a time
+      slot = (slot + 3) & ~3;
       P.cell_slots[c].begin = slot;
       size_t j = 0;  // window position of the sender (senders ascending)
       for (size_t k = 0; k < snd.size(); k += kLaneEdges) {
@@ -142,9 +145,9 @@ void pack_groups(Plan& P, const SmemLayout& L, const PlanInput& in, const std::v
       }
       P.cell_slots[c].count = slot - P.cell_slots[c].begin;
     }
-    const int dummy_slot = slot;
-    w.n_slots = slot;
-    max_slots = std::max(max_slots, slot + 1);
+    const int dummy_slot = (slot + 3) & ~3;  // past the last receiver's 4-slot block
+    w.n_slots = dummy_slot;
+    max_slots = std::max(max_slots, dummy_slot + 1);
     const int ng = (int)(lc.size() + 31) / 32;
     w.n_groups = ng;
     for (int g = 0; g < ng; ++g) {
