@@ -26,6 +26,12 @@ namespace infoli {
 namespace {
 
 constexpr float kNegLog2eOver100 = -0.014426950408889634f;  // -log2(e)/100
+// Stamped plans keep V_dend x kVScale in the window copy and the scaled-V cell
+// array (kVScale^2 = log2(e) / 100): a coupling term's exponent is then
+// -(dV')^2 with dV' = kVScale dV, one multiply less per edge; the partial sums
+// are scaled back once per receiver.
+constexpr float kVScale = 0.12011224087864497f;
+constexpr float kInvVScale = 8.325546111576978f;
 
 // Wait for phase `parity` of an mbarrier, bounded by the launch's timeout.
 __device__ __forceinline__ bool wait_tile(const StepArgs& a, uint64_t* bar, unsigned parity) {
@@ -205,7 +211,7 @@ __device__ __forceinline__ bool poll_finish(const StepArgs& a, const unsigned lo
     for (int k = 0; k < kPollBatch; ++k) {
       if (((b.pend >> k) & 1u) && (unsigned)(b.w[k] >> 32) == want) {
         if (b.dst[k] >= 0) {
-          const float v = __uint_as_float((unsigned)b.w[k]);
+          const float v = __uint_as_float((unsigned)b.w[k]) * kVScale;
           tbuf[b.dst[k]] = v;
           if (dup) tbuf[dup + b.dst[k]] = v;
         }
@@ -254,8 +260,8 @@ __device__ __forceinline__ void couple_packed(const unsigned char* sm, const Sme
       const float gg[4] = {g4.x, g4.y, g4.z, g4.w};
 #pragma unroll
       for (int j = 0; j < 4; ++j) {
-        const float V = vc - *reinterpret_cast<const float*>(sm + off[j]);
-        const float f = fmaf(0.8f, ex2_approx((V * V) * kNegLog2eOver100), 0.2f);
+        const float V = vc - *reinterpret_cast<const float*>(sm + off[j]);  // scaled by kVScale
+        const float f = fmaf(0.8f, ex2_approx(-(V * V)), 0.2f);
         const float term = EDGE_G ? (gg[j] * f) * V : f * V;
         float& acc = (j & 1) ? acc1 : acc0;
         float& cmp = (j & 1) ? cmp1 : cmp0;
@@ -348,6 +354,7 @@ __global__ void __launch_bounds__(BLOCK, 1) step_kernel(const __grid_constant__ 
   float* sVs = sV + cap;
   float* sVa = sV + 2 * cap;
   float* sI = sV + 3 * cap;  // current k of cell r at sI[k * cap + r]
+  float* sVq = sV + kScaledVArray * cap;  // stamped plans: V_dend x kVScale
   float* part = reinterpret_cast<float*>(smem_raw + L.part);
   float* partc = reinterpret_cast<float*>(smem_raw + L.partc);
   uint64_t* mbar = reinterpret_cast<uint64_t*>(smem_raw + L.mbar);
@@ -485,6 +492,7 @@ __global__ void __launch_bounds__(BLOCK, 1) step_kernel(const __grid_constant__ 
   int my_onset = 0, my_off = 0;
   if (owner) {
     sVd[tid] = a.vd[a.step0 & 1][ocell];
+    if (LL) sVq[tid] = sVd[tid] * kVScale;
     sVs[tid] = a.st[F_VS * np + ocell];
     sVa[tid] = a.st[F_VA * np + ocell];
     slots = a.cell_slots[cell];
@@ -569,7 +577,7 @@ __global__ void __launch_bounds__(BLOCK, 1) step_kernel(const __grid_constant__ 
       __syncthreads();
       if (s_abort) break;
       if (prof) t_ready = clock64();
-      couple_packed<KAHAN, EDGE_G>(smem_raw, L, w.n_groups, sVd, part, partc, warp, nwarps, lane);
+      couple_packed<KAHAN, EDGE_G>(smem_raw, L, w.n_groups, sVq, part, partc, warp, nwarps, lane);
       __syncthreads();
     } else if (w.n_tiles > 0) {
       for (int j = 0; j < w.n_tiles; ++j) {
@@ -638,6 +646,7 @@ __global__ void __launch_bounds__(BLOCK, 1) step_kernel(const __grid_constant__ 
         }
         for (; q < slots.y; ++q) ic += ps[q];
       }
+      if (LL) ic *= kInvVScale;  // stamped partial sums are in scaled units
       if (!EDGE_G) ic *= gscale;
       const int ls = step + my_off;
       float iapp;
@@ -667,6 +676,7 @@ __global__ void __launch_bounds__(BLOCK, 1) step_kernel(const __grid_constant__ 
       else if ((int)blockIdx.x != a.stall_cta)
         st_relaxed_gpu_u64(a.vll[(step + 1) & 1] + cell, pack_stamp(v.Vd, (unsigned)(step + 1)));
       sVd[tid] = v.Vd;
+      if (LL) sVq[tid] = v.Vd * kVScale;
       sVs[tid] = v.Vs;
       sVa[tid] = v.Va;
       if (a.trace_every > 0 && (step % a.trace_every) == 0) {

@@ -132,7 +132,10 @@ static inline INFOLI_HD size_t tgather_smem_bytes(SmemShape s) {
 
 // Number of per-cell float arrays kept in shared memory: V_dend, V_soma,
 // V_axon and the nine gate-unit currents.
-enum { kCellArrays = 12 };
+enum { kCellArrays = 13 };
+// Stamped plans: cell array 12 holds V_dend x kVScale of the CTA's own cells
+// (the window copy holds scaled values too; padding entries read it).
+enum { kScaledVArray = 12 };
 // Per-cell gate state in shared memory: 17 float fields (indexed like the
 // device state arrays) plus the FP64 Ca2+ concentration.
 enum { kGateFloats = 17 };

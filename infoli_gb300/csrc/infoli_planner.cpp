@@ -97,7 +97,7 @@ std::vector<TileSpan> make_tiles(const std::vector<int>& u, int cap, int n_pad) 
 // sums stay contiguous and in sender order); the last group of a CTA is
 // filled with dummy chunks that write one spare slot.
 void pack_groups(Plan& P, const SmemLayout& L, const PlanInput& in, const std::vector<std::vector<int>>& win,
-                 int dup_words) {
+                 int dup_words, int cells_cap) {
   const bool edge_g = in.g != nullptr;
   // CTAs are packed in parallel into local tables, then concatenated
   struct Local {
@@ -165,7 +165,7 @@ void pack_groups(Plan& P, const SmemLayout& L, const PlanInput& in, const std::v
           d.x = dummy_slot;
           d.y = 0;
         }
-        pad[l] = (uint16_t)(L.vown + sizeof(float) * (size_t)d.y);
+        pad[l] = (uint16_t)(L.vown + sizeof(float) * ((size_t)kScaledVArray * cells_cap + d.y));
         gdesc.push_back(d);
       }
       // bank-distinct dealing, position by position: lanes whose chunk is
@@ -898,10 +898,10 @@ bool make_plan_base(const PlanInput& in, Plan* out, std::string* err) {
       st.dup_words = dup ? ((w4 + 31) & ~31) + 16 : 0;
       st.tile_cap = dup ? st.dup_words + w4 : w4;
       const SmemLayout SL0 = smem_layout(st);  // tile and cell-array offsets do not depend on the rest
-      const bool offsets_fit = SL0.vown + sizeof(float) * (size_t)cells_cap <= 65536;
+      const bool offsets_fit = SL0.vown + sizeof(float) * (size_t)(kScaledVArray + 1) * cells_cap <= 65536;
       if (in.no_resident || !offsets_fit) continue;
       packed = P;
-      pack_groups(packed, SL0, in, uniq, st.dup_words);
+      pack_groups(packed, SL0, in, uniq, st.dup_words, cells_cap);
       int mg = 1;
       for (const CtaWork& w : packed.cta) mg = std::max(mg, w.n_groups);
       st.max_slots = packed.max_slots;
@@ -1328,6 +1328,9 @@ extern "C" int infoli_plan_emulate(int n, const int64_t* row_ptr, const int32_t*
     std::vector<float> part(P.shape.max_slots, 0.0f);
     float* sVd = reinterpret_cast<float*>(sm.data() + L.vown);
     for (int r = 0; r < w.n_cells; ++r) sVd[r] = vdend[w.cell_begin + r];
+    // stamped plans' padding entries read the scaled-V array; the emulation
+    // runs unscaled, so it holds the plain V_dend here
+    for (int r = 0; r < w.n_cells; ++r) sVd[(size_t)kScaledVArray * P.shape.cells_cap + r] = vdend[w.cell_begin + r];
     if (P.shape.stamped) {
       // the window: the CTA's unique senders, one float each (and the
       // bank-shifted second copy), ids held four per descriptor slot
@@ -1373,7 +1376,7 @@ extern "C" int infoli_plan_emulate(int n, const int64_t* row_ptr, const int32_t*
           for (int k = 0; k < kLaneEdges; ++k) {
             const size_t at = (((size_t)w.group_begin + gi) * kQuads + k / 4) * 32 * 4 + (size_t)l * 4 + k % 4;
             const unsigned off = P.edges[at];
-            if (off % 4 || off + 4 > L.vown + sizeof(float) * (size_t)P.shape.cells_cap) return -7;
+            if (off % 4 || off + 4 > L.vown + sizeof(float) * (size_t)(kScaledVArray + 1) * P.shape.cells_cap) return -7;
             const float V = vc - *reinterpret_cast<const float*>(sm.data() + off);
             const float gg = g ? P.edge_g[at] : 1.0f;
             ((k & 1) ? acc1 : acc0) += (gg * fexp(V)) * V;
