@@ -177,8 +177,8 @@ __device__ __forceinline__ int window_cell(const PollWindow& pw, int i, int* dst
   return pw.cells[i];
 }
 
-// tbuf receives each word at its window index and, when dup > 0, again at
-// dup + index (the bank-shifted second copy).
+// tbuf receives each word's V_dend x kVScale at its window index and, when
+// dup > 0, again at dup + index (the bank-shifted second copy).
 __device__ __forceinline__ void poll_issue(const StepArgs& a, const unsigned long long* src, const PollWindow& pw,
                                            int base, int T, float* tbuf, int dup, PollBatch& b) {
   b.pend = 0;
@@ -558,8 +558,8 @@ __global__ void __launch_bounds__(BLOCK, 1) step_kernel(const __grid_constant__ 
 
     // ---------------- phase A: gap-junction coupling
     if (LL) {
-      // stamped exchange: gather every tile (and the progress probes) once
-      // the words carry this step's stamp, then reduce all chunks.  The
+      // stamped exchange: gather the whole window (and the progress probes)
+      // once the words carry this step's stamp, then reduce all chunks.  The
       // polling threads are the warps without gate units when there are any
       // (they poll while the units compute), else every thread after its units.
       if (tid >= poll_first) {
