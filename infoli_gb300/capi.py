@@ -634,7 +634,10 @@ class Server:
     """Request loop over many simulations on one GPU (infoli_server_* handle)."""
 
     def __init__(self, params, device=0, hbm_budget=0, max_active=0, work_per_cta=0, backfill_ms=0,
-                 prep_threads=0, kahan=False):
+                 prep_threads=0, kahan=False, age_ms=0):
+        """age_ms: prepared requests launch shortest estimated work first, except
+        those submitted more than age_ms ago (oldest first); 0 = 10 s, < 0 =
+        arrival order."""
         L = load()
         self._L = L
         self.params = np.ascontiguousarray(params, dtype=np.float32)[:NPARAM].copy()
@@ -647,6 +650,7 @@ class Server:
         d.backfill_ms = int(backfill_ms)
         d.prep_threads = int(prep_threads)
         d.flags = F_KAHAN if kahan else 0
+        d.age_ms = int(age_ms)
         h = C.c_void_p()
         _check(L.infoli_server_create(C.byref(d), C.byref(h)))
         self._h = h
