@@ -163,6 +163,7 @@ static inline INFOLI_HD SmemLayout smem_layout(SmemShape s) {
   off += (size_t)s.cells_cap * sizeof(double);
   L.gates = off;
   off += (size_t)kGateFloats * (size_t)s.cells_cap * sizeof(float);
+  off = (off + 15) & ~(size_t)15;  // stamped plans read partial slots as float4
   L.part = off;
   off += (size_t)s.max_slots * sizeof(float);
   L.partc = off;
