@@ -138,6 +138,21 @@ __device__ __forceinline__ void store_gates(float* sG, double* sCa, int cap, int
   if (mask & 0x80u) sG[F_XA * cap + r] = g.xa;
 }
 
+// Trace rows fall on the steps that are multiples of trace_every.  A
+// countdown per thread replaces a per-step integer division (it sat on the
+// voltage threads' path every step).
+struct TraceClock {
+  int every, left;
+  __device__ TraceClock(int every_, int step0)
+      : every(every_), left(every_ > 0 ? (every_ - step0 % every_) % every_ : -1) {}
+  // true on a trace step; advances to the next step
+  __device__ bool take() {
+    const bool now = left == 0;
+    if (every > 0) left = now ? every - 1 : left - 1;
+    return now;
+  }
+};
+
 __device__ __forceinline__ unsigned long long pack_stamp(float v, unsigned stamp) {
   return ((unsigned long long)stamp << 32) | (unsigned long long)__float_as_uint(v);
 }
@@ -520,8 +535,10 @@ __global__ void __launch_bounds__(BLOCK, 1) step_kernel(const __grid_constant__ 
     if ((int)blockIdx.x != a.stall_cta)
       st_relaxed_gpu_u64(a.vll[a.step0 & 1] + cell, pack_stamp(sVd[tid], (unsigned)a.step0));
   }
+  TraceClock tclock(a.trace_every, a.step0);
   for (int t = 0; t < a.n_steps; ++t) {
     const int step = a.step0 + t;
+    const bool trace_now = tclock.take();
     const float* vcur = a.vd[step & 1];
     uint64_t t_ready = 0;
 
@@ -679,7 +696,7 @@ __global__ void __launch_bounds__(BLOCK, 1) step_kernel(const __grid_constant__ 
       if (LL) sVq[tid] = v.Vd * kVScale;
       sVs[tid] = v.Vs;
       sVa[tid] = v.Va;
-      if (a.trace_every > 0 && (step % a.trace_every) == 0) {
+      if (trace_now) {
         float* tr = a.trace + (size_t)row * a.trace_nq * np + ocell;
         int qi = 0;
         if (a.trace_mask & TRACE_AXON) tr[(qi++) * np] = v.Va;
@@ -687,7 +704,7 @@ __global__ void __launch_bounds__(BLOCK, 1) step_kernel(const __grid_constant__ 
         if (a.trace_mask & TRACE_DEND) tr[(qi++) * np] = v.Vd;
       }
     }
-    if (a.trace_every > 0 && (step % a.trace_every) == 0) ++row;
+    if (trace_now) ++row;
 
     if (LL) {
       uint64_t t_arrive = prof ? clock64() : 0;
@@ -847,8 +864,10 @@ __global__ void __launch_bounds__(BLOCK, 1) gather_kernel(const __grid_constant_
   unsigned bar_target = 0;
   int row = 0;
   __syncthreads();
+  TraceClock tclock(a.trace_every, a.step0);
   for (int t = 0; t < a.n_steps; ++t) {
     const int step = a.step0 + t;
+    const bool trace_now = tclock.take();
     if (owner) {
       const float* __restrict__ vcur = a.vd[step & 1];
       const float vc = v.Vd;
@@ -898,7 +917,7 @@ __global__ void __launch_bounds__(BLOCK, 1) gather_kernel(const __grid_constant_
       voltage_step(a.P, vk, v, cur, ic, iapp);
       gather_store_gates(sGt, sCa, BLOCK, tid, g);
       a.vd[(step + 1) & 1][cell] = v.Vd;
-      if (a.trace_every > 0 && (step % a.trace_every) == 0) {
+      if (trace_now) {
         float* tr = a.trace + (size_t)row * a.trace_nq * np + cell;
         int qi = 0;
         if (a.trace_mask & TRACE_AXON) tr[(qi++) * np] = v.Va;
@@ -906,7 +925,7 @@ __global__ void __launch_bounds__(BLOCK, 1) gather_kernel(const __grid_constant_
         if (a.trace_mask & TRACE_DEND) tr[(qi++) * np] = v.Vd;
       }
     }
-    if (a.trace_every > 0 && (step % a.trace_every) == 0) ++row;
+    if (trace_now) ++row;
     if (t + 1 < a.n_steps) {
       bar_target += gridDim.x;
       if (!grid_sync(a, bar_target, &s_abort, nullptr)) break;
@@ -999,8 +1018,10 @@ __global__ void __launch_bounds__(BLOCK, 1) tgather_kernel(const __grid_constant
   unsigned bar_target = 0, nload = 0;
   int row = 0;
   __syncthreads();
+  TraceClock tclock(a.trace_every, a.step0);
   for (int t = 0; t < a.n_steps; ++t) {
     const int step = a.step0 + t;
+    const bool trace_now = tclock.take();
     const float* vcur = a.vd[step & 1];
     float acc = 0.0f, comp = 0.0f;
     if (w.n_tiles > 0 && tid == 0) {
@@ -1061,7 +1082,7 @@ __global__ void __launch_bounds__(BLOCK, 1) tgather_kernel(const __grid_constant
       run_units(a.P, 0xffu, v, g, cur);
       voltage_step(a.P, vk, v, cur, ic, iapp);
       a.vd[(step + 1) & 1][cell] = v.Vd;
-      if (a.trace_every > 0 && (step % a.trace_every) == 0) {
+      if (trace_now) {
         float* tr = a.trace + (size_t)row * a.trace_nq * np + cell;
         int qi = 0;
         if (a.trace_mask & TRACE_AXON) tr[(qi++) * np] = v.Va;
@@ -1069,7 +1090,7 @@ __global__ void __launch_bounds__(BLOCK, 1) tgather_kernel(const __grid_constant
         if (a.trace_mask & TRACE_DEND) tr[(qi++) * np] = v.Vd;
       }
     }
-    if (a.trace_every > 0 && (step % a.trace_every) == 0) ++row;
+    if (trace_now) ++row;
     if (t + 1 < a.n_steps) {
       bar_target += gridDim.x;
       if (!grid_sync(a, bar_target, &s_abort, nullptr)) break;
@@ -1212,8 +1233,10 @@ __global__ void __launch_bounds__(BLOCK, 1) bits_kernel(const __grid_constant__ 
   unsigned bar_target = 0, nload = 0;
   int row = 0;
   __syncthreads();
+  TraceClock tclock(a.trace_every, a.step0);
   for (int st = 0; st < a.n_steps; ++st) {
     const int step = a.step0 + st;
+    const bool trace_now = tclock.take();
     const float* vcur = a.vd[step & 1];
     if (owner) sVd[t] = v.Vd;
     if (w.n_tiles > 0 && tid == 0) {
@@ -1277,7 +1300,7 @@ __global__ void __launch_bounds__(BLOCK, 1) bits_kernel(const __grid_constant__ 
       run_units(a.P, 0xffu, v, g, cur);
       voltage_step(a.P, vk, v, cur, ic, iapp);
       a.vd[(step + 1) & 1][cell] = v.Vd;
-      if (a.trace_every > 0 && (step % a.trace_every) == 0) {
+      if (trace_now) {
         float* tr = a.trace + (size_t)row * a.trace_nq * np + cell;
         int qi = 0;
         if (a.trace_mask & TRACE_AXON) tr[(qi++) * np] = v.Va;
@@ -1285,7 +1308,7 @@ __global__ void __launch_bounds__(BLOCK, 1) bits_kernel(const __grid_constant__ 
         if (a.trace_mask & TRACE_DEND) tr[(qi++) * np] = v.Vd;
       }
     }
-    if (a.trace_every > 0 && (step % a.trace_every) == 0) ++row;
+    if (trace_now) ++row;
     if (st + 1 < a.n_steps) {
       bar_target += gridDim.x;
       if (!grid_sync(a, bar_target, &s_abort, nullptr)) break;
