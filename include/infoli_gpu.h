@@ -404,10 +404,13 @@ int infoli_server_destroy(infoli_server* sv);
 /* ------------------------------------------------------------------------ */
 
 /* No counterpart in the reference (its simulator allocates all of its own
- * memory).  For callers that must not allocate device memory while they run
- * the network -- code executing during CUDA stream capture, where cudaMalloc
- * is not allowed, or hosts and language bindings that own every device
- * buffer and hand the library only their own -- this runs n_steps steps
+ * memory).  For callers that must not allocate device memory: a host that
+ * reserved a fixed device-memory arena at start-up and hands out only pieces
+ * of it (an allocation outside the arena can fail or break its budget), a
+ * language binding whose runtime's allocator owns every device buffer (memory
+ * taken behind its back escapes its accounting), or a loop running beside
+ * other GPU work, which cannot take the device-wide synchronisation that
+ * cudaFree (and often cudaMalloc) implies.  This runs n_steps steps
  * without allocating anything: no cudaMalloc / cudaFree, no allocating
  * library call.  Everything is passed in device memory by the caller:
  *   d_row_ptr[n+1], d_col[E], d_g[E] or NULL (then g_uniform on every edge):

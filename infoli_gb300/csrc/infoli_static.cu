@@ -1,10 +1,12 @@
 // Allocation-free entry point: infoli_run_noalloc.
 //
 // Some callers cannot allocate device memory while they drive the
-// simulation: code that runs while a CUDA stream is being captured into a
-// graph (cudaMalloc is not permitted there), hosts with a fixed device-memory
-// budget that hand the library pre-allocated buffers, or foreign-language
-// bindings whose runtime owns every device allocation.  For them this file
+// simulation: hosts that reserved a fixed device-memory arena at start-up and
+// hand the library pieces of it (an allocation outside the arena can fail or
+// break the budget), foreign-language bindings whose runtime's allocator owns
+// every device buffer (memory taken behind its back escapes its accounting),
+// and loops running beside other GPU work that cannot take the device-wide
+// synchronisation cudaFree (and often cudaMalloc) implies.  For them this file
 // offers one entry point that allocates nothing: the caller passes the
 // network, the state and the trace buffer in device memory, and the only
 // scratch the kernel needs -- the V_dend double buffer shared between CTAs,

@@ -1,5 +1,6 @@
 """infoli_run_noalloc: the allocation-free entry point, for callers that may not
-allocate device memory while running (stream capture, caller-owned memory).
+allocate device memory (a fixed device-memory arena, a binding whose allocator
+owns all device buffers, loops that cannot take cudaFree's device-wide sync).
 
 It is checked through the C ABI against the regular entry point
 (infoli_sim_create / infoli_sim_run) on the same network and state, for two
