@@ -261,6 +261,43 @@ __device__ __forceinline__ void couple_packed(const unsigned char* sm, const Sme
   const int2* gd = reinterpret_cast<const int2*>(sm + L.chunks);
   const uint2* ent = reinterpret_cast<const uint2*>(sm + L.edges);
   const float4* gv = reinterpret_cast<const float4*>(sm + L.eg);
+  if (!KAHAN) {
+    // Paired FP32 (f32x2) form: the two accumulators take edges j = 0, 2 and
+    // j = 1, 3 of every quad, so one paired instruction does both.  It runs
+    // on negated values (x - vc = -V exactly; fma(f, -V, -acc) = -fma(f, V,
+    // acc) under round-to-nearest), which needs no paired subtraction, and
+    // flips the sign once per receiver: the same operations in the same
+    // order as the scalar form.
+    const float2 c08 = make_float2(0.8f, 0.8f), c02 = make_float2(0.2f, 0.2f);
+    for (int gi = warp; gi < ngroups; gi += nwarps) {
+      const int2 d = gd[gi * 32 + lane];  // {slot, recv}
+      const float nvc = -sVd[d.y];
+      const float2 nvc2 = make_float2(nvc, nvc);
+      float2 nacc = make_float2(-0.0f, -0.0f);
+#pragma unroll
+      for (int kq = 0; kq < kQuads; ++kq) {
+        const int qi = (gi * kQuads + kq) * 32 + lane;
+        const uint2 o = ent[qi];
+        float4 g4 = make_float4(1.0f, 1.0f, 1.0f, 1.0f);
+        if (EDGE_G) g4 = gv[qi];
+        const unsigned off[4] = {o.x & 0xffffu, o.x >> 16, o.y & 0xffffu, o.y >> 16};
+        const float2 gg[2] = {make_float2(g4.x, g4.y), make_float2(g4.z, g4.w)};
+#pragma unroll
+        for (int h = 0; h < 2; ++h) {
+          const float2 x = make_float2(*reinterpret_cast<const float*>(sm + off[2 * h]),
+                                       *reinterpret_cast<const float*>(sm + off[2 * h + 1]));
+          const float2 nv = __fadd2_rn(x, nvc2);  // -V, scaled by kVScale
+          const float2 sq = __fmul2_rn(nv, nv);
+          const float2 e = make_float2(ex2_approx(-sq.x), ex2_approx(-sq.y));
+          float2 f = __ffma2_rn(c08, e, c02);
+          if (EDGE_G) f = __fmul2_rn(gg[h], f);
+          nacc = __ffma2_rn(f, nv, nacc);
+        }
+      }
+      part[d.x] = -(nacc.x + nacc.y);
+    }
+    return;
+  }
   for (int gi = warp; gi < ngroups; gi += nwarps) {
     const int2 d = gd[gi * 32 + lane];  // {slot, recv}
     const float vc = sVd[d.y];
