@@ -417,7 +417,9 @@ def run_gpu_batched(args, world, rank, local):
     torch.cuda.set_device(local)
     build.build()
     conf, nets, st, meta = batched_workload()
-    bt = ig.Batch(conf, nets, init_state=st, kahan=True, device=local)
+    # cells per CTA picked by the library's autotuner (both shapes timed on a
+    # stratified sample of the networks, before the timed region)
+    bt = ig.Batch(conf, nets, init_state=st, kahan=True, device=local, shape="auto")
     info = bt.info()
     for _ in range(args.warmup):
         bt.run(BATCH_STEP)
@@ -472,7 +474,7 @@ def run_gpu_batched(args, world, rank, local):
     acc_ids = [int(i) for i in np.argsort(meta["sizes"])[:3]]
     acc_nets = [nets[i] for i in acc_ids]
     acc_st = np.concatenate([st[:, off[i]:off[i + 1]] for i in acc_ids], axis=1)
-    with ig.Batch(conf, acc_nets, init_state=acc_st, kahan=True, device=local) as ab:
+    with ig.Batch(conf, acc_nets, init_state=acc_st, kahan=True, device=local, shape=info["block"]) as ab:
         ab.run(ACC_STEPS)
         acc_out = ab.get_state()
         acc_soma = [ab.net_state(acc_out, k)[7] for k in range(len(acc_ids))]
@@ -501,7 +503,7 @@ def run_gpu_batched(args, world, rank, local):
             "n_gpus": world, "steps": args.steps, "warmup": args.warmup,
             "ms_per_step": total_dev_ms / args.steps, "higher_is_better": True, "scaling": "weak",
             "vs_baseline": None, "dtype": "f32", "data": "synthetic",
-            "config": batched_config(meta, {"layout": info, "kahan": True,
+            "config": batched_config(meta, {"layout": info, "kahan": True, "autotune": bt.tune,
                                             "parallelism": f"replicas x{world}" if world > 1 else "single GPU"}),
             "cell_steps_per_s": int(meta["sizes"].sum()) * BATCH_STEP * args.steps * world / (total_dev_ms * 1e-3),
             "edge_evals_per_s": edges * BATCH_STEP * args.steps * world / (total_dev_ms * 1e-3),

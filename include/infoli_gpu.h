@@ -308,6 +308,11 @@ typedef struct {
   const float* g;            /* [n_nets] conductance of every edge of network i */
   int flags;                 /* INFOLI_F_KAHAN */
   int device;
+  /* cells per CTA: 1024 (1,024-thread CTAs, clusters of up to 8) or 512
+   * (512-thread CTAs, clusters of up to 16); 0 = the INFOLI_BATCH_SHAPE
+   * environment variable (512), else 1024.  infoli_batch_autotune picks it
+   * by measurement. */
+  int block;
 } infoli_batch_desc;
 
 /* Uploads the batch and packs it into thread-block clusters.  The stimulus
@@ -332,6 +337,28 @@ int infoli_batch_info(infoli_batch* b, int* ctas, int* cluster, int* block, int6
 int infoli_batch_cta_info(infoli_batch* b, int* max_active_clusters, int32_t* net, int64_t* start_ns,
                           int64_t* end_ns);
 int infoli_batch_destroy(infoli_batch* b);
+
+/* Autotuner of the batch's launch shape (no counterpart in the reference).
+ * It times each CTA shape (desc->block = 1024, then 512) on a trial batch of
+ * a stratified sample of desc's networks (sorted by size, evenly spaced,
+ * the fewest networks whose cells fill every SM twice over at 1,024 cells
+ * per SM, at most max_sample when max_sample > 0), with desc's flags, state
+ * and conductances: one run of trial_steps steps to capture the graph, then
+ * one timed run.  It returns the faster shape in out->block (1024 on a tie)
+ * and the device time per step of each shape; pass out->block as
+ * desc->block to infoli_batch_create.  The trial steps start at step 0, so
+ * they see no stimulus pulse.  desc itself is not modified. */
+typedef struct {
+  int block;            /* the faster shape: 1024 or 512 */
+  int sample_nets;      /* networks in the trial batch */
+  int64_t sample_cells; /* their cells */
+  float ms_per_step[2]; /* trial device time per step: [0] block 1024, [1] block 512 */
+} infoli_batch_tune;
+int infoli_batch_autotune(const infoli_batch_desc* desc, int max_sample, int trial_steps, infoli_batch_tune* out);
+/* The autotuner's sample (host only, no GPU): writes the indices of the
+ * sampled networks, in ascending order, to out_idx[n_nets] and returns their
+ * count, or a negative status. */
+int infoli_batch_tune_sample(int n_nets, const int* n_cells, int max_sample, int64_t target_cells, int* out_idx);
 
 /* ------------------------------------------------------------------------ */
 /* serving: a request loop over many simulations                             */

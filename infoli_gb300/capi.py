@@ -47,7 +47,7 @@ EXPORTED = [
     "infoli_sim_set_stimulus_table", "infoli_gen_bitmask", "infoli_batch_create", "infoli_batch_set_stimulus_pulse",
     "infoli_batch_run", "infoli_batch_get_state", "infoli_batch_set_state", "infoli_batch_info",
     "infoli_batch_cta_info",
-    "infoli_batch_destroy", "infoli_server_create", "infoli_server_submit", "infoli_server_poll",
+    "infoli_batch_destroy", "infoli_batch_autotune", "infoli_batch_tune_sample", "infoli_server_create", "infoli_server_submit", "infoli_server_poll",
     "infoli_server_wait", "infoli_server_status", "infoli_server_destroy",
 ]
 
@@ -85,6 +85,16 @@ class BatchDesc(C.Structure):
         ("g", C.c_void_p),
         ("flags", C.c_int),
         ("device", C.c_int),
+        ("block", C.c_int),
+    ]
+
+
+class BatchTune(C.Structure):
+    _fields_ = [
+        ("block", C.c_int),
+        ("sample_nets", C.c_int),
+        ("sample_cells", C.c_int64),
+        ("ms_per_step", C.c_float * 2),
     ]
 
 
@@ -196,6 +206,8 @@ def load():
         "infoli_batch_info": ([P, P, P, P, P, P], I),
         "infoli_batch_cta_info": ([P, P, P, P, P], I),
         "infoli_batch_destroy": ([P], I),
+        "infoli_batch_autotune": ([C.POINTER(BatchDesc), I, I, C.POINTER(BatchTune)], I),
+        "infoli_batch_tune_sample": ([I, P, I, I64, P], I),
         "infoli_server_create": ([C.POINTER(ServerDesc), C.POINTER(C.c_void_p)], I),
         "infoli_server_submit": ([P, C.POINTER(RequestDesc), P], I),
         "infoli_server_poll": ([P, I64], I),
@@ -542,6 +554,16 @@ def gen_bitmask_csr(n: int, p: float, seed: int):
                      cap_hint=n * (n - 1) * min(1.0, float(p) * 1.05 + 0.002) + 1024)
 
 
+def batch_tune_sample(n_cells, max_sample=0, target_cells=2 * 152 * 1024) -> np.ndarray:
+    """Indices of the networks the batch autotuner times (host only; include/
+    infoli_gpu.h: infoli_batch_tune_sample)."""
+    sizes = np.ascontiguousarray(n_cells, dtype=np.int32)
+    out = np.zeros(sizes.size, dtype=np.int32)
+    m = load().infoli_batch_tune_sample(int(sizes.size), _p(sizes), int(max_sample), int(target_cells), _p(out))
+    _check(min(m, 0))
+    return out[:m].copy()
+
+
 class Batch:
     """Many independent networks in one launch (infoli_batch_* handle).
 
@@ -549,7 +571,11 @@ class Batch:
     init_state: [NSTATE, total] over the networks' cells end to end, or None
     (then init_values is broadcast)."""
 
-    def __init__(self, params, nets, init_state=None, init_values=None, kahan=False, device=0):
+    def __init__(self, params, nets, init_state=None, init_values=None, kahan=False, device=0, shape=0,
+                 tune_steps=200, tune_max_sample=0):
+        """shape: cells per CTA, 1024 or 512; 0 = the library's default;
+        "auto" = infoli_batch_autotune's pick (timed on a sample of the
+        networks, tune_steps steps per shape), kept in self.tune."""
         L = load()
         self._L = L
         params = np.ascontiguousarray(params, dtype=np.float32)
@@ -575,6 +601,15 @@ class Batch:
         d.g = _p(self._g)
         d.flags = F_KAHAN if kahan else 0
         d.device = int(device)
+        self.tune = None
+        if shape == "auto":
+            t = BatchTune()
+            _check(L.infoli_batch_autotune(C.byref(d), int(tune_max_sample), int(tune_steps), C.byref(t)))
+            self.tune = {"block": t.block, "sample_nets": t.sample_nets, "sample_cells": t.sample_cells,
+                         "ms_per_step": {1024: t.ms_per_step[0], 512: t.ms_per_step[1]}}
+            d.block = t.block
+        else:
+            d.block = int(shape)
         h = C.c_void_p()
         _check(L.infoli_batch_create(C.byref(d), C.byref(h)))
         self._h = h

@@ -438,9 +438,15 @@ extern "C" int infoli_batch_create(const infoli_batch_desc* d, infoli_batch** ou
   b->n_nets = d->n_nets;
   b->kahan = (d->flags & INFOLI_F_KAHAN) ? 1 : 0;
   std::memcpy(&b->P, d->params, sizeof(ModelParams));
+  if (d->block != 0 && d->block != 512 && d->block != 1024)
+    return fail(infoli__fail(INFOLI_ERR_ARG, "batch_create: block %d (0, 512 or 1024)", d->block));
   if (cudaSetDevice(b->device) != cudaSuccess) return fail(infoli__fail(INFOLI_ERR_CUDA, "cudaSetDevice failed"));
-  const char* shape_env = getenv("INFOLI_BATCH_SHAPE");
-  b->block = (shape_env && atoi(shape_env) == 512) ? 512 : 1024;
+  if (d->block != 0) {
+    b->block = d->block;
+  } else {
+    const char* shape_env = getenv("INFOLI_BATCH_SHAPE");
+    b->block = (shape_env && atoi(shape_env) == 512) ? 512 : 1024;
+  }
   const int max_cs = b->block == 1024 ? 8 : 16;
   b->cell_base.resize(d->n_nets);
   long long bits_total = 0, in_total = 0;
@@ -698,5 +704,125 @@ extern "C" int infoli_batch_cta_info(infoli_batch* b, int* max_active_clusters, 
 extern "C" int infoli_batch_destroy(infoli_batch* b) {
   infoli__clear_error();
   batch_release(b);
+  return INFOLI_OK;
+}
+
+// ------------------------------------------------------------------ autotuner
+// The launch shape (cells per CTA, and with it the cluster sizes and how many
+// networks share an SM) is picked by timing both shapes on a trial batch.
+// The trial batch is a stratified sample of the networks: sorted by size,
+// m evenly spaced picks, m the smallest count whose cells reach the target
+// (every SM's 1,024 threads twice over), so the trial fills the device like
+// the batch does and covers its size range.
+
+namespace {
+
+int tune_sample(int n_nets, const int* n_cells, int max_sample, long long target_cells, std::vector<int>& out) {
+  std::vector<int> ord(n_nets);
+  for (int i = 0; i < n_nets; ++i) ord[i] = i;
+  std::stable_sort(ord.begin(), ord.end(), [&](int x, int y) { return n_cells[x] < n_cells[y]; });
+  const int cap = max_sample > 0 ? std::min(max_sample, n_nets) : n_nets;
+  for (int m = 1; m <= cap; ++m) {
+    // picks (2k + 1) n_nets / (2m) are distinct because n_nets / m >= 1
+    out.clear();
+    long long cells = 0;
+    for (int k = 0; k < m; ++k) {
+      const int i = ord[(int)(((long long)(2 * k + 1) * n_nets) / (2LL * m))];
+      out.push_back(i);
+      cells += n_cells[i];
+    }
+    if (cells >= target_cells) break;
+  }
+  std::sort(out.begin(), out.end());  // the batch's own order
+  return (int)out.size();
+}
+
+}  // namespace
+
+extern "C" int infoli_batch_tune_sample(int n_nets, const int* n_cells, int max_sample, int64_t target_cells,
+                                        int* out_idx) {
+  infoli__clear_error();
+  if (n_nets <= 0 || !n_cells || !out_idx) return infoli__fail(INFOLI_ERR_ARG, "batch_tune_sample: bad argument");
+  std::vector<int> pick;
+  const int m = tune_sample(n_nets, n_cells, max_sample, (long long)target_cells, pick);
+  std::copy(pick.begin(), pick.end(), out_idx);
+  return m;
+}
+
+extern "C" int infoli_batch_autotune(const infoli_batch_desc* d, int max_sample, int trial_steps,
+                                     infoli_batch_tune* out) {
+  infoli__clear_error();
+  InfoliRange nvtx_range("infoli_batch_autotune");
+  if (!d || !out || d->n_nets <= 0 || !d->n_cells || !d->params || !d->bits || !d->g ||
+      (!d->init_state && !d->init_values) || trial_steps <= 0)
+    return infoli__fail(INFOLI_ERR_ARG, "batch_autotune: bad argument");
+  std::vector<long long> in_base(d->n_nets + 1, 0), cell_base(d->n_nets + 1, 0);
+  for (int i = 0; i < d->n_nets; ++i) {
+    const int n = d->n_cells[i];
+    if (n <= 0 || n > 8192)
+      return infoli__fail(INFOLI_ERR_ARG, "batch_autotune: network %d has %d cells (1 to 8192)", i, n);
+    in_base[i + 1] = in_base[i] + (long long)n * ((n + 31) / 32);
+    cell_base[i + 1] = cell_base[i] + n;
+  }
+  int sms = 0;
+  if (cudaSetDevice(d->device) != cudaSuccess ||
+      cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, d->device) != cudaSuccess)
+    return infoli__fail(INFOLI_ERR_CUDA, "batch_autotune: no CUDA device %d", d->device);
+
+  std::vector<int> pick;
+  tune_sample(d->n_nets, d->n_cells, max_sample, 2LL * sms * 1024, pick);
+  const int m = (int)pick.size();
+  // the trial descriptor: the sampled networks' sizes, bitmasks, conductances
+  // and initial state, laid end to end in the sample's order
+  std::vector<int> sizes(m);
+  std::vector<float> gs(m);
+  long long words = 0, cells = 0;
+  for (int k = 0; k < m; ++k) {
+    sizes[k] = d->n_cells[pick[k]];
+    gs[k] = d->g[pick[k]];
+    words += in_base[pick[k] + 1] - in_base[pick[k]];
+    cells += sizes[k];
+  }
+  std::vector<uint32_t> bits((size_t)words);
+  std::vector<float> st(d->init_state ? (size_t)INFOLI_NSTATE * (size_t)cells : 0);
+  const long long total = cell_base[d->n_nets];
+  long long wo = 0, co = 0;
+  for (int k = 0; k < m; ++k) {
+    const int i = pick[k];
+    std::copy(d->bits + in_base[i], d->bits + in_base[i + 1], bits.begin() + wo);
+    wo += in_base[i + 1] - in_base[i];
+    if (d->init_state)
+      for (int f = 0; f < INFOLI_NSTATE; ++f)
+        std::copy(d->init_state + f * total + cell_base[i], d->init_state + f * total + cell_base[i + 1],
+                  st.begin() + f * cells + co);
+    co += sizes[k];
+  }
+  infoli_batch_desc t = *d;
+  t.n_nets = m;
+  t.n_cells = sizes.data();
+  t.bits = bits.data();
+  t.g = gs.data();
+  t.init_state = d->init_state ? st.data() : nullptr;
+
+  const int shapes[2] = {1024, 512};
+  float ms[2] = {0.0f, 0.0f};
+  for (int s = 0; s < 2; ++s) {
+    t.block = shapes[s];
+    infoli_batch* b = nullptr;
+    int rc = infoli_batch_create(&t, &b);
+    if (rc != INFOLI_OK) return rc;
+    // the first run captures the graph for trial_steps; the second is timed
+    rc = infoli_batch_run(b, trial_steps);
+    if (rc == INFOLI_OK) rc = infoli_batch_run(b, trial_steps);
+    ms[s] = b->last_ms;
+    batch_release(b);  // keeps the error message of a failed run
+    if (rc != INFOLI_OK) return rc;
+  }
+  infoli__clear_error();
+  out->block = ms[1] < ms[0] ? 512 : 1024;
+  out->sample_nets = m;
+  out->sample_cells = cells;
+  out->ms_per_step[0] = ms[0] / (float)trial_steps;
+  out->ms_per_step[1] = ms[1] / (float)trial_steps;
   return INFOLI_OK;
 }

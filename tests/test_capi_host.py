@@ -156,3 +156,50 @@ def test_bitmask_generator_csr_form_matches(built):
         assert not any(r in col[rp[r]:rp[r + 1]] for r in range(n))  # no self edges
         if n > 100:
             assert abs(len(col) / (n * (n - 1)) - p) < 0.01
+
+
+def _tune_sample_py(sizes, max_sample, target):
+    """The batch autotuner's sample, restated: sizes sorted (stable), m evenly
+    spaced picks (2k + 1) N / (2m), m the smallest count reaching target."""
+    n = len(sizes)
+    order = sorted(range(n), key=lambda i: sizes[i])
+    cap = min(max_sample, n) if max_sample > 0 else n
+    for m in range(1, cap + 1):
+        pick = [order[(2 * k + 1) * n // (2 * m)] for k in range(m)]
+        if sum(sizes[i] for i in pick) >= target:
+            break
+    return sorted(pick)
+
+
+def test_batch_tune_sample_is_stratified(capi):
+    rng = np.random.default_rng(3)
+    sizes = np.exp(rng.uniform(np.log(256), np.log(8192), 512)).astype(np.int32)
+    target = 2 * 152 * 1024
+    idx = capi.batch_tune_sample(sizes, target_cells=target)
+    assert list(idx) == _tune_sample_py(list(sizes), 0, target)
+    assert np.all(np.diff(idx) > 0) and idx[0] >= 0 and idx[-1] < sizes.size
+    assert sizes[idx].sum() >= target
+    # the sample spans the size range
+    assert sizes[idx].min() <= np.quantile(sizes, 0.1) and sizes[idx].max() >= np.quantile(sizes, 0.9)
+    # a target no sample reaches takes every network; a zero target the median one
+    assert list(capi.batch_tune_sample(sizes, target_cells=1 << 40)) == list(range(sizes.size))
+    one = capi.batch_tune_sample(sizes, target_cells=0)
+    assert len(one) == 1 and sizes[one[0]] == np.sort(sizes, kind="stable")[sizes.size // 2]
+    capped = capi.batch_tune_sample(sizes, max_sample=10, target_cells=1 << 40)
+    assert list(capped) == _tune_sample_py(list(sizes), 10, 1 << 40) and len(capped) == 10
+
+
+def test_batch_shape_arguments_rejected_without_crashing(capi):
+    conf = capi.read_parameters(CONF)
+    bits = capi.gen_bitmask(100, 0.1, 1)
+    iv = np.ascontiguousarray(conf[23:], dtype=np.float32)
+    with pytest.raises(capi.InfoliError) as e:
+        capi.Batch(conf, [(100, bits, 0.04)], init_values=iv, shape=7)
+    assert e.value.code == capi.ERR_ARG
+    with pytest.raises(capi.InfoliError) as e:
+        capi.Batch(conf, [(100, bits, 0.04)], init_values=iv, shape="auto", tune_steps=0)
+    assert e.value.code == capi.ERR_ARG
+    big = np.zeros((9000, 282), np.uint32)
+    with pytest.raises(capi.InfoliError) as e:
+        capi.Batch(conf, [(9000, big, 0.04)], init_values=iv, shape="auto")
+    assert e.value.code == capi.ERR_ARG

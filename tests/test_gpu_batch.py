@@ -142,3 +142,30 @@ def test_batch_rejects_bad_input(ig, conf):
                  init_values=O.default_state(1, conf)[:, 0])
     with pytest.raises(ig.InfoliError):
         ig.Batch(conf, [(0, bits, 0.04)], init_values=O.default_state(1, conf)[:, 0])
+
+
+def test_batch_autotune_picks_the_faster_shape(ig, conf):
+    """infoli_batch_autotune times both CTA shapes on a sample of the networks
+    (here every network: they hold fewer cells than the sample target); the
+    batch built with its pick equals the batch built with that shape
+    explicitly, bit for bit, and the oracle."""
+    nets, st0, states, csr = _batch_inputs(ig, conf, SIZES, DENS, GS, seed0=31)
+    steps = 500
+    with ig.Batch(conf, nets, init_state=st0, shape="auto", tune_steps=50) as bt:
+        t = bt.tune
+        ms = t["ms_per_step"]
+        assert t["block"] in (512, 1024) and ms[512] > 0 and ms[1024] > 0
+        other = 512 if t["block"] == 1024 else 1024
+        assert ms[t["block"]] <= ms[other]
+        assert t["sample_nets"] == len(nets) and t["sample_cells"] == sum(SIZES)
+        assert bt.info()["block"] == t["block"]
+        bt.run(steps)
+        got = bt.get_state()
+        offsets = bt.offsets
+    with ig.Batch(conf, nets, init_state=st0, shape=t["block"]) as same:
+        same.run(steps)
+        assert np.array_equal(got, same.get_state())
+    for i, (n, _, g) in enumerate(nets):
+        ref, _ = _oracle(conf, n, states[i], *csr[i], g, steps)
+        dvs = np.max(np.abs(got[O.S["V_soma"], offsets[i]:offsets[i + 1]] - ref[O.S["V_soma"]]))
+        assert dvs <= TOL_VSOMA_MV, (i, n, dvs)
