@@ -342,11 +342,11 @@ int infoli_batch_destroy(infoli_batch* b);
  * It times each CTA shape (desc->block = 1024, then 512) on a trial batch of
  * a stratified sample of desc's networks (sorted by size, evenly spaced,
  * the fewest networks whose cells fill every SM twice over at 1,024 cells
- * per SM, at most max_sample when max_sample > 0), with desc's flags, state
- * and conductances: one run of trial_steps steps to capture the graph, then
- * one timed run.  It returns the faster shape in out->block (1024 on a tie)
- * and the device time per step of each shape; pass out->block as
- * desc->block to infoli_batch_create.  The trial steps start at step 0, so
+ * per SM, at most max_sample when max_sample > 0, else at most 4,096), with
+ * desc's flags, state and conductances: one run of trial_steps steps to
+ * capture the graph, then one timed run.  It returns the faster shape in
+ * out->block (1024 on a tie) and the device time per step of each shape;
+ * pass out->block as desc->block to infoli_batch_create.  The trial steps start at step 0, so
  * they see no stimulus pulse.  desc itself is not modified. */
 typedef struct {
   int block;            /* the faster shape: 1024 or 512 */

@@ -712,17 +712,24 @@ extern "C" int infoli_batch_destroy(infoli_batch* b) {
 // networks share an SM) is picked by timing both shapes on a trial batch.
 // The trial batch is a stratified sample of the networks: sorted by size,
 // m evenly spaced picks, m the smallest count whose cells reach the target
-// (every SM's 1,024 threads twice over), so the trial fills the device like
-// the batch does and covers its size range.
+// (every SM's 1,024 threads twice over; m at most 4,096 unless the caller
+// gives a cap), so the trial fills the device like the batch does and covers
+// its size range.
 
 namespace {
+
+constexpr int kTuneMaxSample = 4096;  // sample cap when the caller gives none
 
 int tune_sample(int n_nets, const int* n_cells, int max_sample, long long target_cells, std::vector<int>& out) {
   std::vector<int> ord(n_nets);
   for (int i = 0; i < n_nets; ++i) ord[i] = i;
   std::stable_sort(ord.begin(), ord.end(), [&](int x, int y) { return n_cells[x] < n_cells[y]; });
-  const int cap = max_sample > 0 ? std::min(max_sample, n_nets) : n_nets;
-  for (int m = 1; m <= cap; ++m) {
+  const int cap = std::min(max_sample > 0 ? max_sample : kTuneMaxSample, n_nets);
+  // no sample of fewer than target / (largest network) networks reaches the
+  // target, so the search starts there (the scan costs O(m) per count)
+  long long lo = 1;
+  if (target_cells > 0) lo = (target_cells + n_cells[ord.back()] - 1) / n_cells[ord.back()];
+  for (int m = (int)std::min<long long>(std::max(1LL, lo), cap); m <= cap; ++m) {
     // picks (2k + 1) n_nets / (2m) are distinct because n_nets / m >= 1
     out.clear();
     long long cells = 0;

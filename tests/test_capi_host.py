@@ -163,7 +163,7 @@ def _tune_sample_py(sizes, max_sample, target):
     spaced picks (2k + 1) N / (2m), m the smallest count reaching target."""
     n = len(sizes)
     order = sorted(range(n), key=lambda i: sizes[i])
-    cap = min(max_sample, n) if max_sample > 0 else n
+    cap = min(max_sample if max_sample > 0 else 4096, n)
     for m in range(1, cap + 1):
         pick = [order[(2 * k + 1) * n // (2 * m)] for k in range(m)]
         if sum(sizes[i] for i in pick) >= target:
@@ -187,6 +187,12 @@ def test_batch_tune_sample_is_stratified(capi):
     assert len(one) == 1 and sizes[one[0]] == np.sort(sizes, kind="stable")[sizes.size // 2]
     capped = capi.batch_tune_sample(sizes, max_sample=10, target_cells=1 << 40)
     assert list(capped) == _tune_sample_py(list(sizes), 10, 1 << 40) and len(capped) == 10
+    # many small networks: the default cap bounds the sample (and the search)
+    tiny = np.full(100000, 3, dtype=np.int32)
+    assert len(capi.batch_tune_sample(tiny, target_cells=target)) == 4096
+    mixed = np.concatenate([tiny, [8192]]).astype(np.int32)
+    assert list(capi.batch_tune_sample(mixed, max_sample=300, target_cells=target)) == \
+        _tune_sample_py(list(mixed), 300, target)
 
 
 def test_batch_shape_arguments_rejected_without_crashing(capi):
