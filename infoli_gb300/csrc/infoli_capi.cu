@@ -584,13 +584,9 @@ int infoli_sim_run(infoli_sim* s, int n_steps, int trace_every, int trace_what, 
   int done = 0, li = 0;
   auto drain = [&](const Pending& p) -> int {
     CK(cudaEventSynchronize(s->ev_copy[p.slot]));
-    int row = 0;
-    for (int t = 0; t < n_steps && row < p.rows; ++t) {
-      (void)t;
-    }
     // rows are the multiples of trace_every in the launch's step range
     int st = ((p.step0 + trace_every - 1) / trace_every) * trace_every;
-    for (row = 0; row < p.rows; ++row, st += trace_every) {
+    for (int row = 0; row < p.rows; ++row, st += trace_every) {
       const float* base = s->h_trace[p.slot] + (size_t)row * row_floats;
       int qi = 0;
       for (int bit : {INFOLI_TRACE_AXON, INFOLI_TRACE_SOMA, INFOLI_TRACE_DEND})
