@@ -146,7 +146,7 @@ def test_batch_rejects_bad_input(ig, conf):
 
 def test_batch_autotune_picks_the_faster_shape(ig, conf):
     """infoli_batch_autotune times both CTA shapes on a sample of the networks
-    (here every network: they hold fewer cells than the sample target); the
+    (on a GB300 every network: they hold fewer cells than the sample target); the
     batch built with its pick equals the batch built with that shape
     explicitly, bit for bit, and the oracle."""
     nets, st0, states, csr = _batch_inputs(ig, conf, SIZES, DENS, GS, seed0=31)
@@ -157,7 +157,11 @@ def test_batch_autotune_picks_the_faster_shape(ig, conf):
         assert t["block"] in (512, 1024) and ms[512] > 0 and ms[1024] > 0
         other = 512 if t["block"] == 1024 else 1024
         assert ms[t["block"]] <= ms[other]
-        assert t["sample_nets"] == len(nets) and t["sample_cells"] == sum(SIZES)
+        import torch
+
+        sms = torch.cuda.get_device_properties(0).multi_processor_count
+        expect = ig.batch_tune_sample(SIZES, target_cells=2 * sms * 1024)
+        assert t["sample_nets"] == len(expect) and t["sample_cells"] == sum(SIZES[i] for i in expect)
         assert bt.info()["block"] == t["block"]
         bt.run(steps)
         got = bt.get_state()
