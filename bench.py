@@ -1,30 +1,52 @@
-"""Benchmark: cell-steps/s of the InfOli network update on one GB300 (or N replicas).
-
-Workload (default): 10,000 cells on a 100x100 grid, Gaussian-distance
-connectivity (sigma = 10 cells, candidates within radius 18 = ~1,000 cells per
-receiver, mean degree ~439), uniform g = 0.04, initial V_dend = -60 + U(-1,1) mV
-and g_CaL ~ U(0.6, 0.8) from seed 1, the reference's 6 uA pulse schedule.
-One bench step = one infoli_sim_run call advancing 1,000 explicit-Euler
-timesteps (50 ms simulated) with the V_axon trace streamed to the host every
-100 timesteps, as the reference prints it.  40 bench steps = the 2 s run.
+"""Benchmark: cell-steps/s of the InfOli network update on one GB300 (or N
+replicas), with the batched and served forms measured in the same run.
 
   python bench.py [--gpus N] [--steps K] [--warmup W] [--impl gb300|reference]
+                  [--workload all|grid10k|batched|serving] [--case NAME]
 
-value: cells x timesteps / device time (CUDA events on the simulation's stream,
-state and topology resident in HBM).  e2e: the same work through the C ABI from
-host buffers: per bench step set_state (H2D), run with the trace (D2H), and
-get_state (D2H), wall-clock.  The reference arm times the CPU restatement of
-the reference's OpenMP loop (oracle/, C + OpenMP, all host cores) on a bounded
-sample of the same workload.
+Default line (--workload all), one JSON line with three parts:
+
+* headline (top-level keys): 10,000 cells on a 100x100 grid, Gaussian-distance
+  connectivity (sigma = 10 cells, candidates within radius 18 = ~1,000 cells
+  per receiver, mean degree ~439), uniform g = 0.04, initial V_dend = -60 +
+  U(-1,1) mV and g_CaL ~ U(0.6, 0.8) from seed 1, the reference's 6 uA pulse
+  schedule.  One bench step = one infoli_sim_run call advancing 1,000
+  explicit-Euler timesteps (50 ms simulated) with the V_axon trace streamed to
+  the host every 100 timesteps, as the reference prints it.  `value`: cells x
+  timesteps / device time (CUDA events on the simulation's stream, state and
+  topology resident in HBM, L2 flushed between steps).  `e2e`: the same work
+  through the C ABI from pinned host buffers (set_state H2D, run with the
+  trace D2H, get_state D2H), wall clock.  The line carries the coupling sum's
+  precision mode, the FP64-oracle error, the roofline of the step kernel and
+  the CPU baseline: the reference's own OpenMP build (untouched sources,
+  compiled on this host by oracle/build_ref.sh) timed by its own clock at the
+  same cell count and mean degree, all host cores.
+* "batched": 512 independent networks (sizes log-uniform 256-8,192, density
+  U(0.05, 0.5), g U(0.02, 0.06) per network), the full 10,000 timesteps of
+  every network as 10 graph launches of 1,000 timesteps, launch shape picked by
+  the library's autotuner; against sequential plain runs of every network
+  (infoli_sim, one after another, 1,000 timesteps each) on the same GPU.
+* "serving": a fixed trace of 24 requests arriving as a Poisson stream (mean
+  50/s), sizes log-uniform 500-50,000 cells, durations U(100, 2,000) ms,
+  density U(0.01, 0.30), through the library's request loop; against the same
+  requests run alone one after another (first in, first out) on the same GPU.
+
+--impl reference times the reference's own OpenMP build (or, where it could
+not be built, the oracle's restatement of its loop) on the host cores.
+--case NAME runs one named small case once and prints its device time (the
+commands in profiles/ use these under ncu).
 """
 from __future__ import annotations
 
 import argparse
 import json
 import os
+import re
+import shutil
 import statistics
 import subprocess
 import sys
+import tempfile
 import threading
 import time
 
@@ -34,14 +56,17 @@ sys.path.insert(0, ROOT)
 ROWS, COLS, SIGMA, RADIUS, SEED = 100, 100, 10.0, 18.0, 1
 STEPS_PER_ITER = 1000
 TRACE_EVERY = 100
-CPU_SAMPLE_STEPS = 5000  # about 10 s of the port on 16 host cores
+CPU_SAMPLE_STEPS = 2000  # timesteps of the oracle port, reported beside the reference build
+N_SM_FALLBACK = 152
+SFU_EX2_PER_CLK_SM = 16  # MUFU.EX2 results per clock per SM
+
+CONF_PATH = os.path.join(ROOT, "infoli_gb300", "host", "default.conf")
+REF_DIR = os.path.join(ROOT, "oracle", "_ref")
 
 
 def ncu_traffic():
     """DRAM bytes (read + write) of one step-kernel launch of this workload, from
     the committed ncu summary (profiles/step_kernel_grid10k_stamped.md)."""
-    import re
-
     try:
         with open(os.path.join(ROOT, "profiles", "step_kernel_grid10k_stamped.md")) as f:
             m = re.search(r"traffic \(read \+ write\) per launch \| ([\d,]+) B", f.read())
@@ -64,7 +89,7 @@ def workload():
 
     import infoli_gb300 as ig
 
-    conf = ig.read_parameters(os.path.join(ROOT, "infoli_gb300", "host", "default.conf"))
+    conf = ig.read_parameters(CONF_PATH)
     rp, col = ig.gen_grid_gaussian(ROWS, COLS, SIGMA, RADIUS, SEED)
     n = ROWS * COLS
     st = np.empty((19, n), dtype=np.float32)
@@ -73,6 +98,14 @@ def workload():
     st[0] += rng.uniform(-1, 1, n).astype(np.float32)
     st[6] = rng.uniform(0.6, 0.8, n).astype(np.float32)
     return conf, n, rp, col, st
+
+
+GRID_EDGES = 4391308  # edges of workload()'s grid (the C2 network), checked by the GPU arm
+
+
+def workload_name():
+    """The network both arms run (the same string in both JSON lines)."""
+    return f"grid {ROWS}x{COLS} gaussian sigma={SIGMA} radius={RADIUS} g=0.04 seed=1"
 
 
 class ClockSampler:
@@ -156,6 +189,27 @@ def dist_barrier(world):
         dist.barrier()
 
 
+def host_cpu():
+    """(logical cores, CPU model) of this host."""
+    model = None
+    try:
+        with open("/proc/cpuinfo") as f:
+            txt = f.read()
+        m = re.search(r"model name\s*:\s*(.+)", txt)
+        if m:
+            model = m.group(1).strip()
+    except OSError:
+        pass
+    if model is None:
+        try:
+            out = subprocess.run(["lscpu"], capture_output=True, text=True, timeout=10).stdout
+            m = re.search(r"Model name:\s*(.+)", out)
+            model = m.group(1).strip() if m else None
+        except Exception:
+            model = None
+    return os.cpu_count() or 1, model
+
+
 ACC_STEPS = 2000  # window of the accuracy criterion: max |dV_soma| <= 1e-3 mV over the first 2000 steps
 ACC_TOL_MV = 1e-3
 
@@ -174,9 +228,49 @@ def soma_error_vs_fp64(conf, n, rp, col, st, gpu_soma, g_uniform, threads, final
     return float(np.max(np.abs(np.asarray(gpu_soma, dtype=np.float64) - want)))
 
 
-def workload_name():
-    """The network both arms run (the same string in both JSON lines)."""
-    return f"grid {ROWS}x{COLS} gaussian sigma={SIGMA} radius={RADIUS} g=0.04 seed=1"
+# ------------------------------------------------------- CPU baselines --
+def reference_binary():
+    """The reference's OpenMP build compiled on this host (oracle/_ref), or None."""
+    exe = os.path.join(REF_DIR, "infoli_omp_perf.x")
+    conf = os.path.join(REF_DIR, "default.conf")
+    if os.access(exe, os.X_OK) and os.path.exists(conf):
+        return exe, conf
+    script = os.path.join(ROOT, "oracle", "build_ref.sh")
+    try:
+        subprocess.run(["bash", script], check=True, capture_output=True, timeout=300)
+    except Exception:
+        return None
+    return (exe, conf) if os.access(exe, os.X_OK) else None
+
+
+def reference_sim_steps(sim_ms):
+    """The reference's step count (int)(simTime / DELTA), FP32 (src/openmp/infoli.c:478)."""
+    import numpy as np
+
+    return int(np.float32(sim_ms) / np.float32(0.05))
+
+
+def run_reference_binary(n, p, sim_ms, threads):
+    """One run of the untouched reference OpenMP build: -n n -p p -t sim_ms.
+    Returns (cell-steps/s by its own 'Execution Time for Simulation' clock,
+    src/openmp/infoli.c:428,702,721; that time in s)."""
+    found = reference_binary()
+    if found is None:
+        return None
+    exe, conf = found
+    env = dict(os.environ, OMP_NUM_THREADS=str(threads))
+    d = tempfile.mkdtemp(prefix="infoli_ref_")
+    try:
+        r = subprocess.run([exe, "-n", str(n), "-p", f"{p:.6f}", "-t", str(sim_ms), "-c", conf, "-o",
+                            os.path.join(d, "out.txt")], capture_output=True, text=True, env=env, cwd=d,
+                           timeout=900)
+    finally:
+        shutil.rmtree(d, ignore_errors=True)
+    m = re.search(r"Execution Time for Simulation: ([\d.]+) ms", r.stdout)
+    if r.returncode != 0 or not m:
+        return None
+    t = float(m.group(1)) * 1e-3
+    return n * reference_sim_steps(sim_ms) / t, t
 
 
 def cpu_port_rate(conf, n, rp, col, st, steps, threads):
@@ -191,33 +285,71 @@ def cpu_port_rate(conf, n, rp, col, st, steps, threads):
     return n * steps / dt, dt
 
 
+def grid_stand_in_p(n=ROWS * COLS, edges=GRID_EDGES):
+    """Bernoulli p giving the reference generator the grid's mean degree."""
+    return edges / (n * (n - 1.0))
+
+
 def run_reference(args, world, rank):
+    """Reference arm: the reference's own OpenMP build at the headline's cell
+    count and mean degree (its CLI generates a uniform random network; it cannot
+    express the Gaussian grid), 1,000 timesteps per bench step, timed by its own
+    clock; the oracle port of its loop when the build is unavailable."""
     if rank != 0:
         return 0
-    from oracle import oracle as O
+    n = ROWS * COLS
+    p = grid_stand_in_p()
+    threads, model = host_cpu()
+    sim_ms = STEPS_PER_ITER * 0.05
+    kind = "reference"
+    if reference_binary() is not None:
+        for _ in range(args.warmup):
+            run_reference_binary(n, p, sim_ms, threads)
+        total = 0.0
+        for _ in range(args.steps):
+            r = run_reference_binary(n, p, sim_ms, threads)
+            if r is None:
+                kind = None
+                break
+            total += r[1]
+        steps_per = reference_sim_steps(sim_ms)
+        sample = (f"per bench step one run of the untouched reference OpenMP build (src/openmp/infoli.c + "
+                  f"src/utils/utils.c, gcc -O3 -fopenmp): -n {n} -p {p:.6f} -t {sim_ms:g} = {steps_per} "
+                  f"timesteps, uniform random network with the grid's mean degree, trace every 100 steps, "
+                  f"its own execution-time clock")
+    else:
+        kind = None
+    if kind is None:
+        from oracle import oracle as O
 
-    O.build()
-    conf, n, rp, col, st = workload()
-    threads = os.cpu_count() or 1
-    sample = 100  # timesteps per bench step
-    for _ in range(args.warmup):
-        cpu_port_rate(conf, n, rp, col, st, 10, threads)
-    rates, total = [], 0.0
-    for _ in range(args.steps):
-        r, dt = cpu_port_rate(conf, n, rp, col, st, sample, threads)
-        rates.append(r)
-        total += dt
-    value = n * sample * args.steps / total
+        O.build()
+        import numpy as np
+
+        kind = "port"
+        rp, col = O.gen_uniform(n, p, SEED)
+        conf = O.read_parameters(CONF_PATH)
+        st = O.default_state(n, conf)
+        st[0] += np.random.default_rng(SEED).uniform(-1, 1, n).astype(np.float32)
+        for _ in range(args.warmup):
+            cpu_port_rate(conf, n, rp, col, st, 10, threads)
+        total = 0.0
+        steps_per = 100
+        for _ in range(args.steps):
+            total += cpu_port_rate(conf, n, rp, col, st, steps_per, threads)[1]
+        sample = (f"reference build unavailable on this host; the oracle's restatement of its loop "
+                  f"(oracle/, C + OpenMP), {steps_per} timesteps per bench step, uniform network at p={p:.6f}")
+    value = n * steps_per * args.steps / total
     line = {
         "impl": "reference", "metric": "cell-steps/s", "value": value, "unit": "cell-steps/s",
         "n_gpus": args.gpus, "steps": args.steps, "warmup": args.warmup,
         "ms_per_step": 1e3 * total / args.steps, "higher_is_better": True, "scaling": "weak",
         "vs_baseline": None, "dtype": "f32", "data": "synthetic",
-        "config": {"workload": workload_name(), "cells": n, "edges": int(len(col)),
-                   "mean_degree": float(len(col) / n), "timesteps_per_step": sample,
-                   "trace": f"V_axon every {TRACE_EVERY} timesteps"},
-        "cpu_baseline": {"value": value, "unit": "cell-steps/s", "cores": threads, "kind": "port",
-                         "sample": f"{sample} timesteps of the workload per bench step, OpenMP over cells"},
+        "config": {"workload": workload_name(), "cells": n, "mean_degree": GRID_EDGES / n,
+                   "timesteps_per_step": steps_per, "trace": f"V_axon every {TRACE_EVERY} timesteps",
+                   "topology": "uniform random at the same cell count and mean degree (the reference's "
+                               "generator, src/openmp/infoli.c:337-375)"},
+        "cpu_baseline": {"value": value, "unit": "cell-steps/s", "cores": threads, "cpu": model, "kind": kind,
+                         "sample": sample},
         "e2e": {"value": value, "unit": "cell-steps/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
     }
     print(json.dumps(line))
@@ -233,6 +365,36 @@ def flush_l2():
     torch.cuda.synchronize()
 
 
+def sm_count(local):
+    try:
+        import torch
+
+        return torch.cuda.get_device_properties(local).multi_processor_count
+    except Exception:
+        return N_SM_FALLBACK
+
+
+# ------------------------------------------------------------- headline --
+def time_grid(ig, sim, steps, warmup, local, on_row):
+    """Device-timed bench steps of one Simulation: (per-step ms, launches, clocks, wall)."""
+    import torch
+
+    for _ in range(warmup):
+        sim.run_with_callback(STEPS_PER_ITER, TRACE_EVERY, ig.TRACE_AXON, on_row)
+    dev_ms, launches = [], 0
+    torch.cuda.synchronize()
+    t_wall0 = time.perf_counter()
+    with ClockSampler(local) as clk:
+        for _ in range(steps):
+            flush_l2()
+            sim.run_with_callback(STEPS_PER_ITER, TRACE_EVERY, ig.TRACE_AXON, on_row)
+            ms, nl = sim.last_run_stats()
+            dev_ms.append(ms)
+            launches += nl
+    torch.cuda.synchronize()
+    return dev_ms, launches, clk.summary(), time.perf_counter() - t_wall0
+
+
 def run_gpu(args, world, rank, local):
     import numpy as np
     import torch
@@ -243,33 +405,19 @@ def run_gpu(args, world, rank, local):
     torch.cuda.set_device(local)
     build.build()
     conf, n, rp, col, st = workload()
-    sim = ig.Simulation(n, conf, rp, col, init_state=st, device=local)
+    assert len(col) == GRID_EDGES, len(col)
+    threads, model = host_cpu()
+    kahan = not args.no_kahan
+    sim = ig.Simulation(n, conf, rp, col, init_state=st, device=local, kahan=kahan)
     plan = sim.plan_info()
 
-    rows_holder = {}
-
     def on_row(step, what, v):
-        rows_holder["last"] = (step, v[0])
-
-    # warm-up
-    for _ in range(args.warmup):
-        sim.run_with_callback(STEPS_PER_ITER, TRACE_EVERY, ig.TRACE_AXON, on_row)
+        pass
 
     # ---- device-resident throughput (CUDA events on the simulation stream)
-    dev_ms, launches = [], 0
     dist_barrier(world)
-    torch.cuda.synchronize()
-    t_wall0 = time.perf_counter()
-    with ClockSampler(local) as clk:
-        for _ in range(args.steps):
-            flush_l2()
-            sim.run_with_callback(STEPS_PER_ITER, TRACE_EVERY, ig.TRACE_AXON, on_row)
-            ms, nl = sim.last_run_stats()
-            dev_ms.append(ms)
-            launches += nl
-    torch.cuda.synchronize()
+    dev_ms, launches, clocks, wall = time_grid(ig, sim, args.steps, args.warmup, local, on_row)
     dist_barrier(world)
-    wall = time.perf_counter() - t_wall0
     total_dev_ms = dist_max(sum(dev_ms), world)
 
     # ---- e2e through the C ABI from host buffers
@@ -296,56 +444,100 @@ def run_gpu(args, world, rank, local):
     gpu_soma = sim.run(ACC_STEPS, 1, ig.TRACE_SOMA)["soma"]
     sim.close()
 
+    # ---- the other summation mode, timed the same way (its cost and error)
+    other = None
+    if world == 1:
+        with ig.Simulation(n, conf, rp, col, init_state=st, device=local, kahan=not kahan) as s2:
+            o_ms, o_l, o_clk, _ = time_grid(ig, s2, min(args.steps, 10), min(args.warmup, 3), local, on_row)
+            s2.set_state(st)
+            o_soma = s2.run(ACC_STEPS, 1, ig.TRACE_SOMA)["soma"]
+        other = (o_ms, o_clk, o_soma)
+
     cell_steps = n * STEPS_PER_ITER * args.steps * world
     value = cell_steps / (total_dev_ms * 1e-3)
     e2e_value = cell_steps / e2e_s
 
     # roofline of the dominant kernel (the persistent step kernel): algorithmic
     # bytes per cell-step = 132 B of state + ceil(N/8) B of uniform-g adjacency bits
-    per_launch_steps = STEPS_PER_ITER
-    alg_bytes_per_launch = (132 + (n + 7) // 8) * n * per_launch_steps
+    alg_bytes_per_launch = (132 + (n + 7) // 8) * n * STEPS_PER_ITER
     launch_ms = sum(dev_ms) / max(1, launches)
     achieved = alg_bytes_per_launch / (launch_ms * 1e-3) / 1e9
     peak, peak_kind = peaks()
+    # the bound that applies: the SFU exp2 rate (one exp per edge + 22 per cell)
+    nsm = sm_count(local)
+    mhz = clocks.get("sm_mhz") or 2070.0
+    exps = (len(col) + 22 * n) * STEPS_PER_ITER
+    sfu_ach = exps / (launch_ms * 1e-3)
+    sfu_peak = SFU_EX2_PER_CLK_SM * nsm * mhz * 1e6
 
-    result = None
-    if rank == 0:
-        clocks = clk.summary()
-        threads = os.cpu_count() or 1
-        cpu_rate, cpu_dt = cpu_port_rate(conf, n, rp, col, st, CPU_SAMPLE_STEPS, threads)
-        acc = soma_error_vs_fp64(conf, n, rp, col, st, gpu_soma, conf[1], threads)
-        result = {
-            "metric": "cell-steps/s", "value": value, "unit": "cell-steps/s", "n_gpus": world,
-            "steps": args.steps, "warmup": args.warmup, "ms_per_step": total_dev_ms / args.steps,
-            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
-            "data": "synthetic",
-            "config": {
-                "workload": workload_name(), "cells": n, "edges": int(len(col)), "mean_degree": float(len(col) / n),
-                "timesteps_per_step": STEPS_PER_ITER, "trace": f"V_axon every {TRACE_EVERY} timesteps",
-                "l2": "flushed between timed steps (256 MB memset)",
-                "parallelism": f"replicas x{world}" if world > 1 else "single GPU",
-                "plan": plan,
-            },
-            "e2e": {"value": e2e_value, "unit": "cell-steps/s", "h2d_bytes_per_step": h2d,
-                    "d2h_bytes_per_step": d2h},
-            "gpu_launches": launches,
-            "wall_s": wall,
-            "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
-                         "frac": achieved / peak, "traffic": ncu_traffic(),
-                         "note": f"achieved = algorithmic bytes (132 + N/8 per cell-step) x cells x "
-                                 f"{STEPS_PER_ITER} timesteps over the step kernel's mean launch time "
-                                 f"(CUDA events); peak {peak_kind} HBM copy bandwidth; traffic = ncu "
-                                 f"DRAM read+write of one launch of this workload (profiles/): the "
-                                 f"topology and V_dend windows stay on chip, the step is latency-bound"},
-            "phase_ns_per_timestep": prof["max"],
-            "accuracy": {"max_abs_dV_soma_mV": acc, "steps": ACC_STEPS, "vs": "FP64 oracle (oracle/, same "
-                         "initial state and topology)", "tolerance_mV": ACC_TOL_MV, "pass": acc <= ACC_TOL_MV},
-            "clocks": clocks,
-            "cpu_baseline": {"value": cpu_rate, "unit": "cell-steps/s", "cores": threads, "kind": "port",
-                             "sample": f"{CPU_SAMPLE_STEPS} timesteps of the same workload ({cpu_dt:.1f} s)"},
-        }
-        print(json.dumps(result))
-    return 0
+    if rank != 0:
+        return None
+    cpu = None
+    ref = run_reference_binary(n, grid_stand_in_p(), STEPS_PER_ITER * 0.05, threads)
+    port_rate, port_dt = cpu_port_rate(conf, n, rp, col, st, CPU_SAMPLE_STEPS, threads)
+    if ref is not None:
+        cpu = {"value": ref[0], "unit": "cell-steps/s", "cores": threads, "cpu": model, "kind": "reference",
+               "sample": f"one run of the untouched reference OpenMP build (gcc -O3 -fopenmp, all host threads) "
+                         f"at the same cell count and mean degree (-n {n} -p {grid_stand_in_p():.6f} -t 50 = "
+                         f"1,000 timesteps, uniform random network), its own execution-time clock: "
+                         f"{ref[1]:.2f} s",
+               "port": {"value": port_rate, "sample": f"oracle restatement on the grid itself, "
+                                                      f"{CPU_SAMPLE_STEPS} timesteps ({port_dt:.1f} s)"}}
+    else:
+        cpu = {"value": port_rate, "unit": "cell-steps/s", "cores": threads, "cpu": model, "kind": "port",
+               "sample": f"{CPU_SAMPLE_STEPS} timesteps of the same workload ({port_dt:.1f} s); the reference "
+                         f"build could not be made on this host"}
+    acc = soma_error_vs_fp64(conf, n, rp, col, st, gpu_soma, conf[1], threads)
+    mode = ("kahan: each lane's two FP32 accumulators are Kahan-compensated (paired f32x2), compensated "
+            "partial sums combined per receiver" if kahan else
+            "fp32: two FP32 accumulators per lane (paired f32x2), partial sums per receiver in FP32")
+    result = {
+        "metric": "cell-steps/s", "value": value, "unit": "cell-steps/s", "n_gpus": world,
+        "steps": args.steps, "warmup": args.warmup, "ms_per_step": total_dev_ms / args.steps,
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
+        "data": "synthetic",
+        "config": {
+            "workload": workload_name(), "cells": n, "edges": int(len(col)), "mean_degree": float(len(col) / n),
+            "timesteps_per_step": STEPS_PER_ITER, "trace": f"V_axon every {TRACE_EVERY} timesteps",
+            "l2": "flushed between timed steps (256 MB memset)",
+            "parallelism": f"replicas x{world}" if world > 1 else "single GPU",
+            "plan": plan,
+            "coupling_path": "stamped sender-list plan (topology resident in shared memory as 16-bit "
+                             "window offsets; the planner prefers it to the dense bitmask because every "
+                             "CTA's window fits on chip)",
+        },
+        "precision": {"coupling_sum": mode, "exp": "ex2.approx on the SFU (coupling), expf (gates)",
+                      "ca2plus": "fp64"},
+        "e2e": {"value": e2e_value, "unit": "cell-steps/s", "h2d_bytes_per_step": h2d,
+                "d2h_bytes_per_step": d2h},
+        "gpu_launches": launches,
+        "wall_s": wall,
+        "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
+                     "frac": achieved / peak, "traffic": ncu_traffic(),
+                     "note": f"achieved = algorithmic bytes (132 + N/8 per cell-step) x cells x "
+                             f"{STEPS_PER_ITER} timesteps over the step kernel's mean launch time "
+                             f"(CUDA events); peak {peak_kind} HBM copy bandwidth; traffic = ncu "
+                             f"DRAM read+write of one launch of this workload (profiles/): the "
+                             f"topology and V_dend windows stay on chip, so HBM does not bound the step",
+                     "sfu": {"achieved": sfu_ach, "peak": sfu_peak, "unit": "exp2/s", "frac": sfu_ach / sfu_peak,
+                             "note": f"one ex2 per edge + 22 exps per cell per timestep; peak = "
+                                     f"{SFU_EX2_PER_CLK_SM} per clock per SM x {nsm} SMs x the median SM "
+                                     f"clock sampled ({mhz:.0f} MHz)"}},
+        "phase_ns_per_timestep": prof["max"],
+        "accuracy": {"max_abs_dV_soma_mV": acc, "steps": ACC_STEPS, "vs": "FP64 oracle (oracle/, same "
+                     "initial state and topology)", "tolerance_mV": ACC_TOL_MV, "pass": acc <= ACC_TOL_MV},
+        "clocks": clocks,
+        "cpu_baseline": cpu,
+    }
+    if other is not None:
+        o_ms, o_clk, o_soma = other
+        o_acc = soma_error_vs_fp64(conf, n, rp, col, st, o_soma, conf[1], threads)
+        result["precision"]["other_mode"] = {
+            "coupling_sum": "fp32" if kahan else "kahan",
+            "value": n * STEPS_PER_ITER * len(o_ms) / (sum(o_ms) * 1e-3), "unit": "cell-steps/s",
+            "ms_per_step": sum(o_ms) / len(o_ms), "steps": len(o_ms),
+            "max_abs_dV_soma_mV": o_acc, "clocks": o_clk}
+    return result
 
 
 # ---------------------------------------------------------------- batched --
@@ -356,7 +548,7 @@ def batched_workload():
     import infoli_gb300 as ig
     from infoli_gb300 import workloads
 
-    conf = ig.read_parameters(os.path.join(ROOT, "infoli_gb300", "host", "default.conf"))
+    conf = ig.read_parameters(CONF_PATH)
     nets, st, meta = workloads.batched(conf, n_nets=BATCH_NETS, seed=SEED)
     return conf, nets, st, meta
 
@@ -368,9 +560,8 @@ def batched_config(meta, extra=None):
                     f"{BATCH_TIMESTEPS} timesteps per simulation, {BATCH_STEP} timesteps per bench step",
         "networks": BATCH_NETS, "cells": int(meta["sizes"].sum()), "edges": int(meta["edges"].sum()),
         "timesteps_per_step": BATCH_STEP,
-        "l2": "inputs larger than L2 (bitmasks %.0f MB)" % (meta["edges"].size and
-                                                           sum(int(n) * ((int(n) + 31) // 32) * 4
-                                                               for n in meta["sizes"]) / 1e6),
+        "l2": "inputs larger than L2 (bitmasks %.0f MB)" % (sum(int(n) * ((int(n) + 31) // 32) * 4
+                                                                for n in meta["sizes"]) / 1e6),
     }
     if extra:
         cfg.update(extra)
@@ -407,7 +598,8 @@ def cpu_batched_rate(conf, nets, st, meta, threads, steps=40, k=8):
     return len(nets) / est_batch_s, t_sample, picks
 
 
-def run_gpu_batched(args, world, rank, local):
+def run_gpu_batched(args, world, rank, local, warmup=None):
+    """The batched form (C4): returns its result dict on rank 0."""
     import numpy as np
     import torch
 
@@ -416,20 +608,25 @@ def run_gpu_batched(args, world, rank, local):
 
     torch.cuda.set_device(local)
     build.build()
+    steps = BATCH_TIMESTEPS // BATCH_STEP  # the whole 10,000-timestep simulation of every network
+    warmup = min(args.warmup, 3) if warmup is None else warmup
     conf, nets, st, meta = batched_workload()
-    # cells per CTA picked by the library's autotuner (both shapes timed on a
-    # stratified sample of the networks, before the timed region)
+    # launch shape picked by the library's autotuner (timed on a stratified
+    # sample of the networks, before the timed region)
+    t_tune = time.perf_counter()
     bt = ig.Batch(conf, nets, init_state=st, kahan=True, device=local, shape="auto")
+    t_tune = time.perf_counter() - t_tune
     info = bt.info()
-    for _ in range(args.warmup):
+    for _ in range(warmup):
         bt.run(BATCH_STEP)
+    bt.set_state(st)
     dist_barrier(world)
     torch.cuda.synchronize()
     dev_ms = []
     t_wall0 = time.perf_counter()
     with ClockSampler(local) as clk:
-        for _ in range(args.steps):
-            bt.run(BATCH_STEP)  # one graph launch; inputs (2.5 GB of bitmasks) exceed L2
+        for _ in range(steps):
+            bt.run(BATCH_STEP)  # one graph launch; inputs (588 MB of bitmasks) exceed L2
             dev_ms.append(bt.info()["last_ms"])
     torch.cuda.synchronize()
     dist_barrier(world)
@@ -442,7 +639,7 @@ def run_gpu_batched(args, world, rank, local):
     out_state = torch.empty(st.shape, dtype=torch.float32).pin_memory().numpy()
     dist_barrier(world)
     t0 = time.perf_counter()
-    for _ in range(args.steps):
+    for _ in range(steps):
         bt.set_state(host_state)
         bt.run(BATCH_STEP)
         out_state[:] = bt.get_state()
@@ -450,24 +647,31 @@ def run_gpu_batched(args, world, rank, local):
     finite = float(np.mean([np.isfinite(bt.net_state(out_state, i)).all() for i in range(len(nets))]))
     bt.close()
 
-    sims = len(nets) * world * (BATCH_STEP * args.steps / BATCH_TIMESTEPS)
+    sims = len(nets) * world * (BATCH_STEP * steps / BATCH_TIMESTEPS)
     value = sims / (total_dev_ms * 1e-3)
     e2e_value = sims / e2e_s
     edges = int(meta["edges"].sum())
 
-    # sequential plain runs (one infoli_sim per network, the single-network
-    # path) on a stratified sample, extrapolated to the batch
-    plain_s, picks = 0.0, sample_nets(meta, 8)
+    # sequential plain runs: every network alone through infoli_sim (the
+    # single-network path, each on its auto-selected plan), one after another,
+    # BATCH_STEP timesteps each, the same summation mode
     off = np.concatenate([[0], np.cumsum(meta["sizes"])])
-    for i in picks:
+    plain_dev_s, plain_create_s = 0.0, 0.0
+    t_plain0 = time.perf_counter()
+    for i in range(len(nets)):
         n, bits, g = nets[i]
         rp, col = ig.bitmask_to_csr(n, bits)
+        tc = time.perf_counter()
         with ig.Simulation(n, conf, rp, col, g_uniform=g, init_state=st[:, off[i]:off[i + 1]], kahan=True,
                            device=local) as sim:
-            sim.run(100)
+            plain_create_s += time.perf_counter() - tc
             sim.run(BATCH_STEP)
-            plain_s += sim.last_run_stats()[0] * 1e-3
-    plain_rate = len(nets) / (plain_s * (len(nets) / len(picks)) * (BATCH_TIMESTEPS / BATCH_STEP))
+            plain_dev_s += sim.last_run_stats()[0] * 1e-3
+            sim.get_state()
+    plain_wall_s = time.perf_counter() - t_plain0
+    sims_per_plain_pass = len(nets) * BATCH_STEP / BATCH_TIMESTEPS
+    plain_rate = sims_per_plain_pass / plain_dev_s
+    plain_rate_wall = sims_per_plain_pass / (plain_wall_s - plain_create_s)
 
     # accuracy: the three smallest networks as a batch of their own, ACC_STEPS
     # steps, final V_soma against the FP64 oracle
@@ -479,59 +683,61 @@ def run_gpu_batched(args, world, rank, local):
         acc_out = ab.get_state()
         acc_soma = [ab.net_state(acc_out, k)[7] for k in range(len(acc_ids))]
 
-    result = None
-    if rank == 0:
-        threads = os.cpu_count() or 1
-        acc = 0.0
-        for k, i in enumerate(acc_ids):
-            n_i, bits_i, g_i = nets[i]
-            rp_i, col_i = ig.bitmask_to_csr(n_i, bits_i)
-            acc = max(acc, soma_error_vs_fp64(conf, n_i, rp_i, col_i, st[:, off[i]:off[i + 1]], acc_soma[k], g_i,
-                                              threads, final_only=True))
-        cpu_rate, cpu_t, cpu_picks = cpu_batched_rate(conf, nets, st, meta, threads)
-        # algorithmic bytes of one launch: the bitmask rows once per timestep
-        # (networks whose rows stay in shared memory are still counted) and 132 B
-        # of state per cell-step
-        bits_bytes = sum(int(n) * ((int(n) + 31) // 32) * 4 for n in meta["sizes"])
-        alg = (bits_bytes + 132 * int(meta["sizes"].sum())) * BATCH_STEP
-        launch_ms = sum(dev_ms) / len(dev_ms)
-        achieved = alg / (launch_ms * 1e-3) / 1e9
-        peak, peak_kind = peaks()
-        busy = float((cta["end_ns"] - cta["start_ns"]).sum()) / (152 * float(cta["end_ns"].max()))
-        result = {
-            "metric": "sims/s", "value": value, "unit": "sims/s (10,000-timestep simulations)",
-            "n_gpus": world, "steps": args.steps, "warmup": args.warmup,
-            "ms_per_step": total_dev_ms / args.steps, "higher_is_better": True, "scaling": "weak",
-            "vs_baseline": None, "dtype": "f32", "data": "synthetic",
-            "config": batched_config(meta, {"layout": info, "kahan": True, "autotune": bt.tune,
-                                            "parallelism": f"replicas x{world}" if world > 1 else "single GPU"}),
-            "cell_steps_per_s": int(meta["sizes"].sum()) * BATCH_STEP * args.steps * world / (total_dev_ms * 1e-3),
-            "edge_evals_per_s": edges * BATCH_STEP * args.steps * world / (total_dev_ms * 1e-3),
-            "finite_fraction": finite,
-            "accuracy": {"max_abs_dV_soma_mV": acc, "steps": ACC_STEPS, "networks": acc_ids,
-                         "vs": "FP64 oracle, V_soma after the last step (the batch's three smallest networks run "
-                               "as a batch of their own)", "tolerance_mV": ACC_TOL_MV, "pass": acc <= ACC_TOL_MV},
-            "sequential_plain": {"value": plain_rate, "unit": "sims/s", "sample": f"networks {picks}, "
-                                 f"{BATCH_STEP} timesteps each through infoli_sim (Kahan), device time, "
-                                 f"extrapolated to {len(nets)} networks x {BATCH_TIMESTEPS} timesteps"},
-            "e2e": {"value": e2e_value, "unit": "sims/s", "h2d_bytes_per_step": int(st.nbytes),
-                    "d2h_bytes_per_step": int(st.nbytes)},
-            # per bench step: one launch per cluster-size group + the step-index advance
-            "gpu_launches": args.steps * (len({(int(n) + info["block"] - 1) // info["block"]
-                                               for n in meta["sizes"]}) + 1),
-            "wall_s": wall,
-            "sm_busy_fraction": busy,
-            "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
-                         "frac": achieved / peak, "traffic": None,
-                         "note": f"achieved = bitmask bytes + 132 B per cell-step per timestep over the mean "
-                                 f"launch time; peak {peak_kind} HBM copy bandwidth; the batched kernel is "
-                                 f"issue-bound (bit extraction + SFU exp per edge), not HBM-bound"},
-            "clocks": clk.summary(),
-            "cpu_baseline": {"value": cpu_rate, "unit": "sims/s", "cores": threads, "kind": "port",
-                             "sample": f"networks {cpu_picks} x 40 timesteps ({cpu_t:.1f} s), extrapolated"},
-        }
-        print(json.dumps(result))
-    return 0
+    if rank != 0:
+        return None
+    threads, model = host_cpu()
+    acc = 0.0
+    for k, i in enumerate(acc_ids):
+        n_i, bits_i, g_i = nets[i]
+        rp_i, col_i = ig.bitmask_to_csr(n_i, bits_i)
+        acc = max(acc, soma_error_vs_fp64(conf, n_i, rp_i, col_i, st[:, off[i]:off[i + 1]], acc_soma[k], g_i,
+                                          threads, final_only=True))
+    cpu_rate, cpu_t, cpu_picks = cpu_batched_rate(conf, nets, st, meta, threads)
+    # algorithmic bytes of one launch: the bitmask rows once per timestep
+    # (networks whose rows stay in shared memory are still counted) and 132 B
+    # of state per cell-step
+    bits_bytes = sum(int(n) * ((int(n) + 31) // 32) * 4 for n in meta["sizes"])
+    alg = (bits_bytes + 132 * int(meta["sizes"].sum())) * BATCH_STEP
+    launch_ms = sum(dev_ms) / len(dev_ms)
+    achieved = alg / (launch_ms * 1e-3) / 1e9
+    peak, peak_kind = peaks()
+    nsm = sm_count(local)
+    busy = float((cta["end_ns"] - cta["start_ns"]).sum()) / (nsm * float(cta["end_ns"].max()))
+    return {
+        "metric": "sims/s", "value": value, "unit": "sims/s (10,000-timestep simulations)",
+        "steps": steps, "warmup": warmup, "ms_per_step": total_dev_ms / steps, "higher_is_better": True,
+        "config": batched_config(meta, {"layout": info, "kahan": True, "autotune": bt.tune,
+                                        "autotune_s": t_tune}),
+        "cell_steps_per_s": int(meta["sizes"].sum()) * BATCH_STEP * steps * world / (total_dev_ms * 1e-3),
+        "edge_evals_per_s": edges * BATCH_STEP * steps * world / (total_dev_ms * 1e-3),
+        "finite_fraction": finite,
+        "accuracy": {"max_abs_dV_soma_mV": acc, "steps": ACC_STEPS, "networks": acc_ids,
+                     "vs": "FP64 oracle, V_soma after the last step (the batch's three smallest networks run "
+                           "as a batch of their own)", "tolerance_mV": ACC_TOL_MV, "pass": acc <= ACC_TOL_MV},
+        "sequential_plain": {
+            "value": plain_rate, "unit": "sims/s", "value_wall": plain_rate_wall,
+            "sample": f"all {len(nets)} networks, one after another through infoli_sim (Kahan, each on its "
+                      f"auto-selected plan), {BATCH_STEP} timesteps each: device time {plain_dev_s:.2f} s "
+                      f"(value), wall time without creation {plain_wall_s - plain_create_s:.2f} s "
+                      f"(value_wall), creation {plain_create_s:.2f} s; the batched bench step is the same "
+                      f"{BATCH_STEP} timesteps of every network",
+            "speedup_batched_vs_plain": value / plain_rate},
+        "e2e": {"value": e2e_value, "unit": "sims/s", "h2d_bytes_per_step": int(st.nbytes),
+                "d2h_bytes_per_step": int(st.nbytes)},
+        # per bench step: one launch per cluster-size group + the step-index advance
+        "gpu_launches": steps * (len({(int(n) + info["block"] - 1) // info["block"]
+                                      for n in meta["sizes"]}) + 1),
+        "wall_s": wall,
+        "sm_busy_fraction": busy,
+        "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
+                     "frac": achieved / peak, "traffic": None,
+                     "note": f"achieved = bitmask bytes + 132 B per cell-step per timestep over the mean "
+                             f"launch time; peak {peak_kind} HBM copy bandwidth; the batched kernel is "
+                             f"issue-bound (bit extraction + SFU exp per edge), not HBM-bound"},
+        "clocks": clk.summary(),
+        "cpu_baseline": {"value": cpu_rate, "unit": "sims/s", "cores": threads, "cpu": model, "kind": "port",
+                         "sample": f"networks {cpu_picks} x 40 timesteps ({cpu_t:.1f} s), extrapolated"},
+    }
 
 
 def run_reference_batched(args, world, rank):
@@ -541,7 +747,7 @@ def run_reference_batched(args, world, rank):
 
     O.build()
     conf, nets, st, meta = batched_workload()
-    threads = os.cpu_count() or 1
+    threads, model = host_cpu()
     rates = []
     for _ in range(args.warmup):
         cpu_batched_rate(conf, nets, st, meta, threads, steps=2, k=2)
@@ -556,7 +762,7 @@ def run_reference_batched(args, world, rank):
         "n_gpus": args.gpus, "steps": args.steps, "warmup": args.warmup,
         "ms_per_step": 1e3 * t_total / args.steps, "higher_is_better": True, "scaling": "weak",
         "vs_baseline": None, "dtype": "f32", "data": "synthetic", "config": batched_config(meta),
-        "cpu_baseline": {"value": value, "unit": "sims/s", "cores": threads, "kind": "port",
+        "cpu_baseline": {"value": value, "unit": "sims/s", "cores": threads, "cpu": model, "kind": "port",
                          "sample": f"per bench step networks {picks} x 5 timesteps, extrapolated"},
         "e2e": {"value": value, "unit": "sims/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
     }
@@ -592,7 +798,8 @@ def serving_requests(conf, count, seed=SEED):
     return t, reqs
 
 
-def run_gpu_serving(args, world, rank, local):
+def run_gpu_serving(args, world, rank, local, count=SERVE_REQUESTS, warmup=None):
+    """The served form (C5): returns its result dict on rank 0."""
     import numpy as np
     import torch
 
@@ -601,14 +808,14 @@ def run_gpu_serving(args, world, rank, local):
 
     torch.cuda.set_device(local)
     build.build()
-    conf = ig.read_parameters(os.path.join(ROOT, "infoli_gb300", "host", "default.conf"))
-    count = args.steps
+    warmup = min(args.warmup, 3) if warmup is None else warmup
+    conf = ig.read_parameters(CONF_PATH)
     arrivals, reqs = serving_requests(conf, count)
     work = np.array([len(r["col"]) * r["n_steps"] for r in reqs], dtype=np.float64)
     with ig.Server(conf, device=local, kahan=True) as sv:
         # warm-up: small requests through the same server
         wu = [sv.submit(n=r["n"], row_ptr=r["row_ptr"], col=r["col"], n_steps=200, g_uniform=0.04,
-                        init_state=r["init_state"]) for r in sorted(reqs, key=lambda r: r["n"])[:args.warmup]]
+                        init_state=r["init_state"]) for r in sorted(reqs, key=lambda r: r["n"])[:warmup]]
         for i in wu:
             sv.wait(i, want_state=False)
         dist_barrier(world)
@@ -644,46 +851,85 @@ def run_gpu_serving(args, world, rank, local):
     seq_lat = np.array(seq_lat)
     seq_rate = count / finish
 
-    result = None
-    if rank == 0:
-        in_bytes = sum(r["row_ptr"].nbytes + r["col"].nbytes + r["init_state"].nbytes for r in reqs)
-        result = {
-            "metric": "served sims/s", "value": served, "unit": "sims/s", "n_gpus": world, "steps": count,
-            "warmup": args.warmup, "ms_per_step": 1e3 * makespan / count, "higher_is_better": True,
-            "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
-            "config": {"workload": f"Poisson request stream, mean {SERVE_RATE:g}/s, {count} requests (one per "
-                                   f"bench step), sizes log-uniform 500-50000 cells, durations U(100,2000) ms, "
-                                   f"density U(0.01,0.30), g=0.04, admitted by HBM budget (80% of free memory)",
-                       "requests": count, "cells": [r["n"] for r in reqs], "steps": [r["n_steps"] for r in reqs],
-                       "edges": [int(len(r["col"])) for r in reqs],
-                       "scheduling": "admission first in first out by HBM budget (up to 64 admitted); prepared "
-                                     "requests launch shortest estimated work (edges x steps) first, any "
-                                     "submitted more than 10 s ago ahead of them; SM share one CTA per 32768 "
-                                     "edge evaluations per step",
-                       "timing": "host wall clock from the first "
-                       "arrival to the last result (serving is end to end)", "l2": "inputs larger than L2"},
-            "latency_s": {"p50": float(np.percentile(lat, 50)), "p99": float(np.percentile(lat, 99)),
-                          "max": float(lat.max())},
-            "sequential_plain": {"value": seq_rate, "unit": "sims/s",
-                                 "latency_s": {"p50": float(np.percentile(seq_lat, 50)),
-                                               "p99": float(np.percentile(seq_lat, 99))},
-                                 "sample": "every request alone through infoli_sim (create+run+read), FIFO "
-                                           "schedule on the same arrivals"},
-            "offered_edge_evals_per_s": float(work.sum() / max(arrivals[-1], 1e-9)),
-            "sustained_edge_evals_per_s": float(work.sum() / makespan),
-            "e2e": {"value": served, "unit": "sims/s", "h2d_bytes_per_step": int(in_bytes / count),
-                    "d2h_bytes_per_step": int(sum(19 * 4 * r["n"] for r in reqs) / count)},
-            "grid_per_request": [i["grid"] for i in infos],
-            "prep_queue_s_per_request": [round(i["prep_start_s"] - i["admit_s"], 3) for i in infos],
-            "prepare_s_per_request": [round(i["prepared_s"] - i["prep_start_s"], 3) for i in infos],
-            "launch_wait_s_per_request": [round(i["start_s"] - i["prepared_s"], 3) for i in infos],
-            "run_s_per_request": [round(i["done_s"] - i["start_s"], 3) for i in infos],
-            "plain_service_s_per_request": [round(x, 3) for x in service],
-            "plain_create_s_per_request": [round(x, 3) for x in plain_create],
-            "gpu_launches": int(sum((r["n_steps"] + 8191) // 8192 for r in reqs)),
-            "clocks": clk.summary(),
-        }
-        print(json.dumps(result))
+    if rank != 0:
+        return None
+    in_bytes = sum(r["row_ptr"].nbytes + r["col"].nbytes + r["init_state"].nbytes for r in reqs)
+    return {
+        "metric": "served sims/s", "value": served, "unit": "sims/s", "steps": count,
+        "warmup": warmup, "ms_per_step": 1e3 * makespan / count, "higher_is_better": True,
+        "config": {"workload": f"Poisson request stream, mean {SERVE_RATE:g}/s, {count} requests (one per "
+                               f"bench step), sizes log-uniform 500-50000 cells, durations U(100,2000) ms, "
+                               f"density U(0.01,0.30), g=0.04, admitted by HBM budget (80% of free memory)",
+                   "requests": count, "cells": [r["n"] for r in reqs], "timesteps": [r["n_steps"] for r in reqs],
+                   "edges": [int(len(r["col"])) for r in reqs],
+                   "arrivals_s": [round(float(a), 4) for a in arrivals],
+                   "timing": "host wall clock from the first arrival to the last result (serving is end to end)",
+                   "l2": "inputs larger than L2"},
+        "latency_s": {"p50": float(np.percentile(lat, 50)), "p99": float(np.percentile(lat, 99)),
+                      "max": float(lat.max())},
+        "sequential_plain": {"value": seq_rate, "unit": "sims/s",
+                             "latency_s": {"p50": float(np.percentile(seq_lat, 50)),
+                                           "p99": float(np.percentile(seq_lat, 99))},
+                             "sample": "every request alone through infoli_sim (create+run+read), measured one "
+                                       "after another; first-in-first-out schedule on the same arrivals"},
+        "offered_edge_evals_per_s": float(work.sum() / max(arrivals[-1], 1e-9)),
+        "sustained_edge_evals_per_s": float(work.sum() / makespan),
+        "e2e": {"value": served, "unit": "sims/s", "h2d_bytes_per_step": int(in_bytes / count),
+                "d2h_bytes_per_step": int(sum(19 * 4 * r["n"] for r in reqs) / count)},
+        "placement_per_request": [i["grid"] for i in infos],
+        "prepare_s_per_request": [round(i["prepared_s"] - i["prep_start_s"], 3) for i in infos],
+        "launch_wait_s_per_request": [round(i["start_s"] - i["prepared_s"], 3) for i in infos],
+        "run_s_per_request": [round(i["done_s"] - i["start_s"], 3) for i in infos],
+        "plain_service_s_per_request": [round(x, 3) for x in service],
+        "gpu_launches": int(sum((r["n_steps"] + 8191) // 8192 for r in reqs)),
+        "clocks": clk.summary(),
+    }
+
+
+# ------------------------------------------------------------------ cases --
+CASES = ("grid10k", "uniform1k", "dense10k", "sparse100k", "batch64")
+
+
+def run_case(name, steps):
+    """One named small case, run once; prints its device time.  Seeded inputs:
+      grid10k    the headline workload (10,000-cell Gaussian grid), stamped plan
+      uniform1k  1,000 cells, the reference generator at p = 0.1
+      dense10k   10,000 cells, bitmask generator at p = 0.2 (coupling-dominated)
+      sparse100k 100,000 cells, 100 senders each, per-edge g U(0.02, 0.06)
+      batch64    the first 64 networks of the batched workload, one graph launch"""
+    import numpy as np
+
+    import infoli_gb300 as ig
+    from infoli_gb300 import build, workloads
+
+    build.build()
+    conf = ig.read_parameters(CONF_PATH)
+    if name == "batch64":
+        nets, st, meta = workloads.batched(conf, n_nets=64, seed=1)
+        with ig.Batch(conf, nets, init_state=st, kahan=True) as bt:
+            bt.run(steps)
+            print(f"batch64: {int(meta['sizes'].sum())} cells, {int(meta['edges'].sum())} edges, {bt.info()}")
+        return 0
+    rng = np.random.default_rng(1)
+    g = None
+    if name == "grid10k":
+        _, n, rp, col, st = workload()
+    else:
+        if name == "uniform1k":
+            n = 1000
+            rp, col = ig.gen_uniform(n, 0.1, 1)
+        elif name == "dense10k":
+            n = 10000
+            rp, col = ig.gen_bitmask_csr(n, 0.2, 5)
+        else:
+            n = 100000
+            rp, col, g = ig.gen_fixed_degree(n, 100, 3, (0.02, 0.06))
+        st = workloads.perturbed_state(conf, n, rng)
+    with ig.Simulation(n, conf, rp, col, g=g, init_state=st, kahan=True) as sim:
+        sim.run(steps)
+        ms, launches = sim.last_run_stats()
+        print(f"{name}: {n} cells, {len(col)} edges, plan {sim.plan_info()}, {steps} steps in {ms:.3f} ms "
+              f"({launches} launches)")
     return 0
 
 
@@ -691,26 +937,49 @@ def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
     ap.add_argument("--steps", type=int, default=None)
-    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--warmup", type=int, default=5)
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
-    ap.add_argument("--workload", default="grid10k", choices=["grid10k", "batched", "serving"])
+    ap.add_argument("--workload", default="all", choices=["all", "grid10k", "batched", "serving"])
+    ap.add_argument("--case", choices=CASES, default=None)
+    ap.add_argument("--no-kahan", action="store_true", help="headline with the uncompensated coupling sum")
     args = ap.parse_args()
+    if args.case:
+        return run_case(args.case, args.steps or 100)
     if args.steps is None:
-        args.steps = {"grid10k": 40, "batched": 10, "serving": SERVE_REQUESTS}[args.workload]
+        args.steps = {"all": 20, "grid10k": 20, "batched": 10, "serving": SERVE_REQUESTS}[args.workload]
     world, rank, local = dist_setup()
-    if args.workload == "serving":
-        if args.impl == "reference":
-            print(json.dumps({"impl": "reference", "unavailable": "the reference has no serving mode; its "
-                              "per-request CPU cost is the grid10k reference arm"}))
-            return 0
-        return run_gpu_serving(args, world, rank, local)
-    if args.workload == "batched":
-        if args.impl == "reference":
-            return run_reference_batched(args, world, rank)
-        return run_gpu_batched(args, world, rank, local)
     if args.impl == "reference":
+        if args.workload == "serving":
+            print(json.dumps({"impl": "reference", "unavailable": "the reference has no serving mode; its "
+                              "per-request CPU cost is the headline reference arm"}))
+            return 0
+        if args.workload == "batched":
+            return run_reference_batched(args, world, rank)
         return run_reference(args, world, rank)
-    return run_gpu(args, world, rank, local)
+    if args.workload == "batched":
+        res = run_gpu_batched(args, world, rank, local, warmup=args.warmup)
+        if res is not None:
+            res.update({"n_gpus": world, "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic"})
+            print(json.dumps(res))
+        return 0
+    if args.workload == "serving":
+        res = run_gpu_serving(args, world, rank, local, count=args.steps, warmup=args.warmup)
+        if res is not None:
+            res.update({"n_gpus": world, "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic"})
+            print(json.dumps(res))
+        return 0
+    line = run_gpu(args, world, rank, local)
+    if args.workload == "all":
+        # the batched and served forms on the same GPU, in the same run (one
+        # replica per GPU under torchrun: the sub-objects are rank 0's own)
+        bres = run_gpu_batched(args, world, rank, local)
+        sres = run_gpu_serving(args, world, rank, local)
+        if line is not None:
+            line["batched"] = bres
+            line["serving"] = sres
+    if line is not None:
+        print(json.dumps(line))
+    return 0
 
 
 if __name__ == "__main__":

@@ -448,8 +448,22 @@ int infoli_server_destroy(infoli_server* sv);
  *   d_trace_axon[n_steps * n] or NULL: V_axon after every step.
  * The stimulus is one global pulse (pulse_amp for pulse_start <= step <
  * pulse_end; the reference's default is 20000, 20499, 6).  step0 is the index
- * of the first step.  `stream` is a cudaStream_t (NULL: the default stream);
- * the call returns after the run has finished on it.
+ * of the first step; step0 + n_steps must not exceed INT_MAX.  `stream` is a
+ * cudaStream_t (NULL: the default stream); the call returns after the run has
+ * finished on it, having synchronised that stream only.
+ * Topology contract: d_row_ptr[0..n] non-decreasing from d_row_ptr[0] >= 0,
+ * and d_row_ptr[n] no larger than the length of d_col and d_g.  A decreasing
+ * or negative row_ptr, a sender id outside [0, n) or a NULL d_col with edges
+ * is detected on the device, skipped without reading outside the arrays, and
+ * returned as INFOLI_ERR_ARG; d_row_ptr[n] beyond the caller's arrays cannot
+ * be detected.
+ * Precision between calls: Ca2Plus is carried in FP64 on the device during a
+ * call but d_state holds FP32, so each call ends by rounding it to FP32.  Two
+ * chained calls therefore differ from one call of the same total length in
+ * the last bits of Ca2Plus (and what follows from them), unlike
+ * infoli_sim_run, which keeps the FP64 value between runs.
+ * Device waits (the grid barrier) give up after INFOLI_WAIT_TIMEOUT_MS
+ * (default 4000 ms) and return INFOLI_ERR_TIMEOUT.
  * The only scratch (V_dend double buffer, barrier counter, error word) is a
  * static device array of fixed size in the library, so networks are limited
  * to 65536 cells (INFOLI_ERR_CAPACITY beyond).  Every GPU that loads the

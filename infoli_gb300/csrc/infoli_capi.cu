@@ -19,6 +19,13 @@
 
 using namespace infoli;
 
+extern "C" unsigned long long infoli__wait_timeout_ns(void) {
+  const char* s = getenv("INFOLI_WAIT_TIMEOUT_MS");
+  long ms = s ? atol(s) : 4000;
+  if (ms <= 0) ms = 4000;
+  return (unsigned long long)ms * 1000000ull;
+}
+
 #define CK(call)                                                                                    \
   do {                                                                                              \
     cudaError_t e_ = (call);                                                                        \
@@ -32,13 +39,6 @@ namespace {
 constexpr int kThreads = 1024;
 constexpr int kMaxStepsPerLaunch = 8192;
 constexpr size_t kTraceSlotBytes = 64u << 20;
-
-unsigned long long wait_timeout_ns() {
-  const char* s = getenv("INFOLI_WAIT_TIMEOUT_MS");
-  long ms = s ? atol(s) : 4000;
-  if (ms <= 0) ms = 4000;
-  return (unsigned long long)ms * 1000000ull;
-}
 
 // Device memory of simulation handles comes from one stream-ordered pool per
 // device (cudaMallocFromPoolAsync / cudaFreeAsync on the handle's stream).
@@ -253,7 +253,7 @@ int fill_args(infoli_sim* s, StepArgs* a) {
   a->stim_dur = s->stim_dur;
   a->bar = s->d_bar;
   a->err = s->d_err;
-  a->timeout_ns = wait_timeout_ns();
+  a->timeout_ns = infoli__wait_timeout_ns();
   // failure-detection test hook (see StepArgs::stall_cta); unset in normal use
   const char* stall = getenv("INFOLI_STALL_CTA");
   a->stall_cta = stall ? atoi(stall) : -1;

@@ -14,6 +14,10 @@ int infoli__fail(int code, const char* fmt, ...)
     ;
 void infoli__clear_error(void);
 
+/* Limit of every bounded device-side wait, in ns: INFOLI_WAIT_TIMEOUT_MS
+ * (default 4000 ms). */
+unsigned long long infoli__wait_timeout_ns(void);
+
 #ifdef __cplusplus
 }
 

@@ -298,37 +298,57 @@ __device__ __forceinline__ void couple_packed(const unsigned char* sm, const Sme
     }
     return;
   }
-  for (int gi = warp; gi < ngroups; gi += nwarps) {
-    const int2 d = gd[gi * 32 + lane];  // {slot, recv}
-    const float vc = sVd[d.y];
-    float acc0 = 0.0f, acc1 = 0.0f, cmp0 = 0.0f, cmp1 = 0.0f;
+  {
+    // Kahan-compensated paired form.  Same sign trick: the accumulators hold
+    // -sum while the compensations c hold +c, so each Kahan step
+    //   y = term - c,  s = acc + y,  c = (s - acc) - y,  acc = s
+    // becomes, on negated terms nt = -term and nacc = -acc,
+    //   ny = fma(f, -V, c),  ns = nacc + ny,  c = ny - (ns - nacc)
+    // (each an exact negation of the scalar step under round-to-nearest; the
+    // subtractions are fma with -1, which rounds once like a subtraction).
+    // The two accumulators are merged with an error-free TwoSum whose error
+    // joins the compensation, so the lane's partial and its compensation
+    // carry the whole chunk.
+    const float2 c08 = make_float2(0.8f, 0.8f), c02 = make_float2(0.2f, 0.2f);
+    const float2 m1 = make_float2(-1.0f, -1.0f);
+    for (int gi = warp; gi < ngroups; gi += nwarps) {
+      const int2 d = gd[gi * 32 + lane];  // {slot, recv}
+      const float nvc = -sVd[d.y];
+      const float2 nvc2 = make_float2(nvc, nvc);
+      float2 nacc = make_float2(-0.0f, -0.0f);
+      float2 cmp = make_float2(0.0f, 0.0f);
 #pragma unroll
-    for (int kq = 0; kq < kQuads; ++kq) {
-      const int qi = (gi * kQuads + kq) * 32 + lane;
-      const uint2 o = ent[qi];
-      float4 g4 = make_float4(1.0f, 1.0f, 1.0f, 1.0f);
-      if (EDGE_G) g4 = gv[qi];
-      const unsigned off[4] = {o.x & 0xffffu, o.x >> 16, o.y & 0xffffu, o.y >> 16};
-      const float gg[4] = {g4.x, g4.y, g4.z, g4.w};
+      for (int kq = 0; kq < kQuads; ++kq) {
+        const int qi = (gi * kQuads + kq) * 32 + lane;
+        const uint2 o = ent[qi];
+        float4 g4 = make_float4(1.0f, 1.0f, 1.0f, 1.0f);
+        if (EDGE_G) g4 = gv[qi];
+        const unsigned off[4] = {o.x & 0xffffu, o.x >> 16, o.y & 0xffffu, o.y >> 16};
+        const float2 gg[2] = {make_float2(g4.x, g4.y), make_float2(g4.z, g4.w)};
 #pragma unroll
-      for (int j = 0; j < 4; ++j) {
-        const float V = vc - *reinterpret_cast<const float*>(sm + off[j]);  // scaled by kVScale
-        const float f = fmaf(0.8f, ex2_approx(-(V * V)), 0.2f);
-        const float term = EDGE_G ? (gg[j] * f) * V : f * V;
-        float& acc = (j & 1) ? acc1 : acc0;
-        float& cmp = (j & 1) ? cmp1 : cmp0;
-        if (KAHAN) {
-          const float y = term - cmp;
-          const float s = acc + y;
-          cmp = (s - acc) - y;
-          acc = s;
-        } else {
-          acc += term;
+        for (int h = 0; h < 2; ++h) {
+          const float2 x = make_float2(*reinterpret_cast<const float*>(sm + off[2 * h]),
+                                       *reinterpret_cast<const float*>(sm + off[2 * h + 1]));
+          const float2 nv = __fadd2_rn(x, nvc2);  // -V, scaled by kVScale
+          const float2 sq = __fmul2_rn(nv, nv);
+          const float2 e = make_float2(ex2_approx(-sq.x), ex2_approx(-sq.y));
+          float2 f = __ffma2_rn(c08, e, c02);
+          if (EDGE_G) f = __fmul2_rn(gg[h], f);
+          const float2 ny = __ffma2_rn(f, nv, cmp);      // -(term - c)
+          const float2 ns = __fadd2_rn(nacc, ny);        // -(acc + y)
+          const float2 dt = __ffma2_rn(nacc, m1, ns);    // ns - nacc
+          cmp = __ffma2_rn(dt, m1, ny);                  // ny - (ns - nacc) = (s - acc) - y
+          nacc = ns;
         }
       }
+      // TwoSum of the two accumulators (values un-negated)
+      const float a0 = -nacc.x, a1 = -nacc.y;
+      const float sum = a0 + a1;
+      const float bb = sum - a0;
+      const float err = (a0 - (sum - bb)) + (a1 - bb);  // a0 + a1 = sum + err exactly
+      part[d.x] = sum;
+      partc[d.x] = (cmp.x + cmp.y) - err;
     }
-    part[d.x] = acc0 + acc1;
-    if (KAHAN) partc[d.x] = cmp0 + cmp1;
   }
 }
 

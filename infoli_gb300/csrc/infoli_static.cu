@@ -17,9 +17,16 @@
 // The kernel is a variant of the persistent step kernel: one thread per cell
 // runs the coupling sum straight from the CSR lists (gathering V_dend from
 // the shared scratch buffer) and the fused compartment update with
-// register-resident state, with one grid barrier per step.
+// register-resident state, with one grid barrier per step.  The barrier
+// counter is 64-bit, so one call may run any number of steps without it
+// wrapping.  Malformed topology (a sender id outside [0, n), a NULL column
+// array with edges, a decreasing or negative row_ptr) is recorded in the
+// error word and the bad read is skipped, so it never reads outside the
+// caller's buffers through a bad index; row_ptr[n] itself cannot be checked
+// against the length of the caller's arrays and is the caller's contract.
 #include <cuda_runtime.h>
 
+#include <climits>
 #include <cstdint>
 #include <cstring>
 #include <mutex>
@@ -36,8 +43,10 @@ constexpr int kNoAllocMaxCells = 65536;  // largest network the static scratch h
 constexpr int kNoAllocBlock = 512;
 constexpr int kMaxDevices = 64;
 
-// Scratch layout: [0, 256) barrier counter + error word (zeroed before every
-// launch); [256, ...) V_dend double buffer, 2 x kNoAllocMaxCells floats.
+// Scratch layout: [0, 256) 64-bit barrier counter at 0 + error word at 64
+// (zeroed before every launch); [256, ...) V_dend double buffer,
+// 2 x kNoAllocMaxCells floats.
+constexpr int kErrBarrier = 1, kErrSender = 2, kErrRowPtr = 3;
 constexpr size_t kCtlBytes = 256;
 constexpr size_t kScratchBytes = kCtlBytes + 2 * sizeof(float) * (size_t)kNoAllocMaxCells;
 static __device__ __align__(256) unsigned char g_noalloc_scratch[kScratchBytes];
@@ -59,17 +68,18 @@ struct NoAllocArgs {
   unsigned long long timeout_ns;
 };
 
-__device__ __forceinline__ bool noalloc_barrier(const NoAllocArgs& a, unsigned* bar, int* err, unsigned target) {
+__device__ __forceinline__ bool noalloc_barrier(const NoAllocArgs& a, unsigned long long* bar, int* err,
+                                                unsigned long long target) {
   __shared__ int s_abort;
   __syncthreads();
   if (threadIdx.x == 0) {
     s_abort = 0;
     __threadfence();
-    red_release_gpu_add(bar, 1u);
+    red_release_gpu_add_u64(bar, 1ull);
     const uint64_t t0 = globaltimer_ns();
-    while (ld_acquire_gpu(bar) < target) {
+    while (ld_acquire_gpu_u64(bar) < target) {
       if (ld_relaxed_gpu(err) != 0 || globaltimer_ns() - t0 > a.timeout_ns) {
-        atomicCAS(err, 0, 1);
+        atomicCAS(err, 0, kErrBarrier);
         s_abort = 1;
         break;
       }
@@ -80,7 +90,7 @@ __device__ __forceinline__ bool noalloc_barrier(const NoAllocArgs& a, unsigned* 
 }
 
 __global__ void __launch_bounds__(kNoAllocBlock, 1) noalloc_step_kernel(const __grid_constant__ NoAllocArgs a) {
-  unsigned* bar = reinterpret_cast<unsigned*>(a.scratch);
+  unsigned long long* bar = reinterpret_cast<unsigned long long*>(a.scratch);
   int* err = reinterpret_cast<int*>(a.scratch + 64);
   float* vd[2] = {reinterpret_cast<float*>(a.scratch + kCtlBytes),
                   reinterpret_cast<float*>(a.scratch + kCtlBytes) + kNoAllocMaxCells};
@@ -118,18 +128,31 @@ __global__ void __launch_bounds__(kNoAllocBlock, 1) noalloc_step_kernel(const __
     gs.xa = s[18 * N + c];
     vd[a.step0 & 1][c] = v.Vd;
   }
-  unsigned target = gridDim.x;
+  unsigned long long target = gridDim.x;
   bool ok = noalloc_barrier(a, bar, err, target);
+  // this thread's edge range, checked once (a bad row is recorded and skipped)
+  int64_t e_begin = 0, e_end = 0;
+  if (own) {
+    e_begin = a.row_ptr[c];
+    e_end = a.row_ptr[c + 1];
+    if (e_begin < 0 || e_end < e_begin) {
+      atomicCAS(err, 0, kErrRowPtr);
+      e_end = e_begin;
+    } else if (e_end > e_begin && a.col == nullptr) {
+      atomicCAS(err, 0, kErrSender);
+      e_end = e_begin;
+    }
+  }
   const VoltCoef vk = volt_coef(a.P);
   for (int t = 0; t < a.n_steps && ok; ++t) {
     const int step = a.step0 + t;
     if (own) {
       const float* vcur = vd[step & 1];
       float acc = 0.0f;
-      for (int64_t e = a.row_ptr[c]; e < a.row_ptr[c + 1]; ++e) {
+      for (int64_t e = e_begin; e < e_end; ++e) {
         const int s = a.col[e];
         if ((unsigned)s >= (unsigned)n) {  // malformed topology: record, never read outside the buffer
-          atomicCAS(err, 0, 2);
+          atomicCAS(err, 0, kErrSender);
           continue;
         }
         const float V = v.Vd - __ldcg(vcur + s);  // L2: written by other CTAs this launch
@@ -184,6 +207,8 @@ extern "C" int infoli_run_noalloc(const float* params, int n_cells, const int64_
   infoli__clear_error();
   if (!params || !d_row_ptr || !d_state || n_cells <= 0 || n_steps < 0 || step0 < 0)
     return infoli__fail(INFOLI_ERR_ARG, "run_noalloc: bad argument");
+  if ((long long)step0 + (long long)n_steps > (long long)INT_MAX)
+    return infoli__fail(INFOLI_ERR_ARG, "run_noalloc: step0 + n_steps exceeds INT_MAX");
   if (n_cells > kNoAllocMaxCells)
     return infoli__fail(INFOLI_ERR_CAPACITY,
                         "run_noalloc: %d cells exceed the static scratch limit of %d cells; use infoli_sim_create",
@@ -206,10 +231,14 @@ extern "C" int infoli_run_noalloc(const float* params, int n_cells, const int64_
     scratch = g_scratch_addr[dev];
   }
   int nsm = 0;
-  cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev);
+  e = cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev);
+  if (e != cudaSuccess)
+    return infoli__fail(INFOLI_ERR_CUDA, "run_noalloc: cudaDeviceGetAttribute: %s", cudaGetErrorString(e));
   const int grid = (n_cells + kNoAllocBlock - 1) / kNoAllocBlock;
   int per_sm = 0;
-  cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, noalloc_step_kernel, kNoAllocBlock, 0);
+  e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, noalloc_step_kernel, kNoAllocBlock, 0);
+  if (e != cudaSuccess)
+    return infoli__fail(INFOLI_ERR_CUDA, "run_noalloc: occupancy query: %s", cudaGetErrorString(e));
   if (grid > per_sm * nsm)
     return infoli__fail(INFOLI_ERR_CAPACITY, "run_noalloc: %d CTAs cannot be co-resident (%d allowed)", grid,
                         per_sm * nsm);
@@ -229,7 +258,7 @@ extern "C" int infoli_run_noalloc(const float* params, int n_cells, const int64_
   a.state = d_state;
   a.trace_axon = d_trace_axon;
   a.scratch = scratch;
-  a.timeout_ns = 4000ull * 1000000ull;
+  a.timeout_ns = infoli__wait_timeout_ns();
   cudaStream_t s = static_cast<cudaStream_t>(stream);
   // the barrier counter and the error word must start at zero
   e = cudaMemsetAsync(scratch, 0, kCtlBytes, s);
@@ -237,12 +266,16 @@ extern "C" int infoli_run_noalloc(const float* params, int n_cells, const int64_
   void* args[] = {&a};
   e = cudaLaunchCooperativeKernel((const void*)noalloc_step_kernel, dim3(grid), dim3(kNoAllocBlock), args, 0, s);
   if (e != cudaSuccess) return infoli__fail(INFOLI_ERR_CUDA, "run_noalloc: launch: %s", cudaGetErrorString(e));
+  // the error word comes back on the caller's stream: a plain cudaMemcpy would
+  // go to the legacy default stream and wait for every blocking stream
+  int err = 0;
+  e = cudaMemcpyAsync(&err, scratch + 64, sizeof(int), cudaMemcpyDeviceToHost, s);
+  if (e != cudaSuccess) return infoli__fail(INFOLI_ERR_CUDA, "run_noalloc: %s", cudaGetErrorString(e));
   e = cudaStreamSynchronize(s);
   if (e != cudaSuccess) return infoli__fail(INFOLI_ERR_CUDA, "run_noalloc: %s", cudaGetErrorString(e));
-  int err = 0;
-  e = cudaMemcpy(&err, scratch + 64, sizeof(int), cudaMemcpyDeviceToHost);
-  if (e != cudaSuccess) return infoli__fail(INFOLI_ERR_CUDA, "run_noalloc: %s", cudaGetErrorString(e));
-  if (err == 2) return infoli__fail(INFOLI_ERR_ARG, "run_noalloc: a sender id is outside [0, n_cells)");
+  if (err == kErrSender)
+    return infoli__fail(INFOLI_ERR_ARG, "run_noalloc: a sender id is outside [0, n_cells) (or d_col is NULL)");
+  if (err == kErrRowPtr) return infoli__fail(INFOLI_ERR_ARG, "run_noalloc: d_row_ptr is negative or decreasing");
   if (err) return infoli__fail(INFOLI_ERR_TIMEOUT, "run_noalloc: grid barrier wait gave up");
   return INFOLI_OK;
 }

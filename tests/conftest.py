@@ -29,3 +29,16 @@ def conf():
     from infoli_gb300 import capi
 
     return capi.read_parameters(os.path.join(ROOT, "infoli_gb300", "host", "default.conf"))
+
+
+def pytest_sessionstart(session):
+    # measured figures the at-size parity tests print in the terminal summary
+    session.config._infoli_report = []
+
+
+def pytest_terminal_summary(terminalreporter, exitstatus, config):
+    lines = getattr(config, "_infoli_report", [])
+    if lines:
+        terminalreporter.section("measured against the oracle")
+        for line in lines:
+            terminalreporter.write_line(line)

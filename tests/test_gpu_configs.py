@@ -1,0 +1,161 @@
+"""The benchmark configurations themselves, at their stated sizes, on the GPU
+against the float oracle (the reference's FP32 arithmetic restated,
+src/openmp/infoli.c:482-485 stimulus, :496-520 coupling, :548-679 cell update):
+
+  C1  1,000 cells, the reference generator at p = 0.1 (seed 1), g = 0.04, the
+      heterogeneous twin (V_dend -60 + U(-1, 1), g_CaL U(0.6, 0.8)), 2 s =
+      40,000 steps through the reference's 6 uA pulse at steps 20,000-20,498;
+  C2  the bench's 10,000-cell Gaussian grid (sigma 10, radius 18), the same
+      pulse, 2 s;
+  C3  100,000 cells x 100 senders drawn uniformly, g ~ U(0.02, 0.06) per edge,
+      per-cell pulses of amplitude U(0, 8) uA/cm2 with onsets U(0, 500) ms
+      lasting 5 ms (100 steps), 1 s = 20,000 steps.
+
+Criteria (the path's stated accuracy): max |dV_soma| <= 1e-3 mV over the first
+2,000 steps, and soma spike steps (upward crossings of 0 mV) equal within one
+step.  Both runs go chunk by chunk (state carried, V_soma every step) so the
+full-length traces never sit in memory.  The measured figures are printed in
+the terminal summary.
+"""
+import os
+import sys
+
+import numpy as np
+import pytest
+
+from helpers import CONF, TOL_SPIKE_STEPS, TOL_VSOMA_MV, hetero_state
+from oracle import oracle as O
+
+pytestmark = pytest.mark.gpu
+
+ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+
+
+@pytest.fixture(scope="module")
+def ig(built):
+    import infoli_gb300
+
+    assert infoli_gb300.device_count() >= 1
+    return infoli_gb300
+
+
+@pytest.fixture(scope="module")
+def conf(built):
+    return O.read_parameters(CONF)
+
+
+class SpikeLog:
+    """Upward 0 mV crossings of V_soma, per cell, streamed chunk by chunk."""
+
+    def __init__(self, n):
+        self.prev = None
+        self.steps = []  # (cell, step) pairs, appended per chunk
+        self.n = n
+
+    def add(self, soma, step0):
+        v = soma if self.prev is None else np.vstack([self.prev[None, :], soma])
+        first = step0 + (0 if self.prev is None else -1)
+        r, c = np.nonzero((v[:-1] < 0.0) & (v[1:] >= 0.0))
+        self.steps.append(np.stack([c, first + r + 1], axis=1))
+        self.prev = soma[-1].copy()
+
+    def per_cell(self):
+        a = np.concatenate(self.steps) if self.steps else np.zeros((0, 2), np.int64)
+        a = a[np.lexsort((a[:, 1], a[:, 0]))]
+        out = [[] for _ in range(self.n)]
+        for c, s in a:
+            out[c].append(int(s))
+        return out
+
+
+def spike_agreement(gs, rs, tol=TOL_SPIKE_STEPS):
+    """(spikes in the oracle run, cells whose trains differ in count or by > tol steps)."""
+    bad = 0
+    for x, y in zip(gs, rs):
+        if len(x) != len(y) or (len(x) and np.max(np.abs(np.asarray(x) - np.asarray(y))) > tol):
+            bad += 1
+    return sum(len(y) for y in rs), bad
+
+
+def run_both(ig, conf, n, rp, col, st0, steps, chunk, g=None, stim=None, whole=None):
+    """GPU and float oracle side by side over `steps`, `chunk` steps at a time.
+    Returns (max |dV_soma| over the first 2,000 steps, GPU spikes, oracle spikes);
+    `whole`, a dict, receives max |dV_soma| over every step as "max_all"."""
+    sim = ig.Simulation(n, conf, rp, col, g=g, init_state=st0)
+    if stim is not None:
+        sim.set_stimulus_cells(stim[1], stim[2], stim[3])
+    st = st0.copy()
+    logs = (SpikeLog(n), SpikeLog(n))
+    err, t = 0.0, 0
+    threads = O.max_threads()
+    while t < steps:
+        k = min(chunk, steps - t)
+        gs = sim.run(k, 1, ig.TRACE_SOMA)["soma"]
+        rs = O.run(n, conf[:23], st, rp, col, g=g, g_uniform=conf[1], stim=stim, step0=t, nsteps=k,
+                   trace_every=1, traces=("soma",), nthreads=threads)["soma"]
+        if t < 2000:
+            m = min(k, 2000 - t)
+            err = max(err, float(np.max(np.abs(gs[:m] - rs[:m]))))
+        if whole is not None:
+            whole["max_all"] = max(whole.get("max_all", 0.0), float(np.max(np.abs(gs - rs))))
+        logs[0].add(gs, t)
+        logs[1].add(rs, t)
+        t += k
+    sim.close()
+    return err, logs[0].per_cell(), logs[1].per_cell()
+
+
+def _report(request, name, err, gsp, rsp, extra=""):
+    total, bad = spike_agreement(gsp, rsp)
+    line = (f"{name}: max|dV_soma| over 2,000 steps {err:.3e} mV (<= {TOL_VSOMA_MV:g}); oracle spikes {total}, "
+            f"GPU spikes {sum(len(x) for x in gsp)}, cells whose spike steps differ by > {TOL_SPIKE_STEPS} step "
+            f"or in count: {bad} of {len(rsp)}{extra}")
+    request.config._infoli_report.append(line)
+    print(line)
+    return total, bad
+
+
+def test_c1_uniform_1k_two_seconds_heterogeneous(ig, conf, request):
+    n = 1000
+    rp, col = ig.gen_uniform(n, 0.1, 1)
+    st0 = hetero_state(conf, n, 1)
+    err, gsp, rsp = run_both(ig, conf, n, rp, col, st0, 40000, 5000)
+    total, bad = _report(request, "C1 1,000 cells p=0.1, 40,000 steps", err, gsp, rsp)
+    assert err <= TOL_VSOMA_MV
+    assert total > 0  # the pulse makes the cells spike
+    assert bad == 0
+
+
+def test_c2_grid10k_spike_steps_two_seconds(ig, conf, request):
+    sys.path.insert(0, ROOT)
+    import bench
+
+    cfg, n, rp, col, st0 = bench.workload()
+    err, gsp, rsp = run_both(ig, cfg, n, rp, col, st0, 40000, 2000)
+    # the spec window: 1 s simulated from the pulse onset (steps 20,000-39,999)
+    first_s = [[s for s in x if s < 20000] for x in rsp]
+    total, bad = _report(request, "C2 10k grid, 40,000 steps", err, gsp, rsp,
+                         extra=f"; oracle spikes before step 20,000: {sum(len(x) for x in first_s)}")
+    assert err <= TOL_VSOMA_MV
+    assert total > 0
+    assert bad == 0
+
+
+def test_c3_sparse100k_per_cell_pulses(ig, conf, request):
+    n, k = 100000, 100
+    rp, col, g = ig.gen_fixed_degree(n, k, 3, (0.02, 0.06))
+    rng = np.random.default_rng(3)
+    amp = rng.uniform(0.0, 8.0, n).astype(np.float32)
+    onset = rng.integers(0, 10000, n).astype(np.int32)
+    stim = ("cell", amp, onset, 100)
+    st0 = hetero_state(conf, n, 3)
+    whole = {}
+    err, gsp, rsp = run_both(ig, conf, n, rp, col, st0, 20000, 500, g=g, stim=stim, whole=whole)
+    total, bad = _report(request, "C3 100k x 100 CSR, per-edge g, per-cell pulses, 20,000 steps", err, gsp, rsp,
+                         extra=f"; max|dV_soma| over all 20,000 steps {whole['max_all']:.3e} mV")
+    assert err <= TOL_VSOMA_MV
+    assert bad == 0
+    # U(0, 8) uA/cm2 for 5 ms stays below threshold, so no cell spikes and the
+    # whole second is a subthreshold trajectory: it must stay as close as the
+    # first 2,000 steps do, to the stated tolerance
+    assert whole["max_all"] <= TOL_VSOMA_MV

@@ -62,14 +62,22 @@ def test_noalloc_matches_regular_entry_point_two_calls(env, per_edge_g):
     d_state = _dev(torch, st0.reshape(-1))
     d_tr = torch.zeros(steps * n, dtype=torch.float32, device="cuda")
     lib = ig.capi.load()
-    got = []
+    got, free_before, free_after = [], None, None
+    torch.cuda.synchronize()
     for call in range(2):
+        if call == 1:
+            # the second call must leave the device's free memory unchanged
+            # (the first may still be the library's first use on this device)
+            free_before = torch.cuda.mem_get_info()[0]
         rc = lib.infoli_run_noalloc(params.ctypes.data_as(C.c_void_p), n, _ptr(d_rp), _ptr(d_col), _ptr(d_g),
                                     float(conf[1]), 150, 450, 1.0, _ptr(d_state), call * steps, steps,
                                     _ptr(d_tr), None)
+        if call == 1:
+            free_after = torch.cuda.mem_get_info()[0]
         assert rc == 0, lib.infoli_last_error()
         got.append(d_tr.cpu().numpy().reshape(steps, n).copy())
     state = d_state.cpu().numpy().reshape(19, n)
+    assert free_after == free_before, (free_before, free_after)
 
     d1, d2 = np.max(np.abs(got[0] - ref1)), np.max(np.abs(got[1] - ref2))
     assert d1 <= 10 * TOL_VSOMA_MV and d2 <= 10 * TOL_VSOMA_MV, (d1, d2)
@@ -90,3 +98,39 @@ def test_noalloc_rejects_networks_beyond_the_static_limit(env):
                                 _ptr(d_state), 0, 1, None, None)
     assert rc == ig.capi.ERR_CAPACITY
     assert b"65536" in lib.infoli_last_error()
+
+
+def test_noalloc_reports_malformed_topology_then_runs_clean(env):
+    """A sender id outside [0, n) and a decreasing row_ptr are caught on the
+    device (the bad read is skipped) and returned as INFOLI_ERR_ARG; the next
+    call on the same buffers, with the topology repaired, succeeds."""
+    ig, torch, conf = env
+    n, steps = 64, 20
+    rp, col = ig.gen_uniform(n, 0.2, 5)
+    st0 = hetero_state(conf, n, 6)
+    params = np.ascontiguousarray(conf[:23], dtype=np.float32)
+    lib = ig.capi.load()
+    d_rp, d_col = _dev(torch, rp), _dev(torch, col)
+    d_state = _dev(torch, st0.reshape(-1))
+
+    def call():
+        return lib.infoli_run_noalloc(params.ctypes.data_as(C.c_void_p), n, _ptr(d_rp), _ptr(d_col), None,
+                                      float(conf[1]), 0, 0, 0.0, _ptr(d_state), 0, steps, None, None)
+
+    bad_col = col.copy()
+    bad_col[len(col) // 2] = n
+    d_col.copy_(torch.from_numpy(bad_col))
+    assert call() == ig.capi.ERR_ARG
+    assert b"sender id" in lib.infoli_last_error()
+
+    d_col.copy_(torch.from_numpy(col))
+    bad_rp = rp.copy()
+    bad_rp[n // 2] = bad_rp[n // 2 + 1] + 1  # row n/2 - 1 grows, row n/2 runs backwards
+    d_rp.copy_(torch.from_numpy(bad_rp))
+    assert call() == ig.capi.ERR_ARG
+    assert b"row_ptr" in lib.infoli_last_error()
+
+    d_rp.copy_(torch.from_numpy(rp))
+    d_state.copy_(torch.from_numpy(st0.reshape(-1)))
+    assert call() == 0, lib.infoli_last_error()
+    assert np.isfinite(d_state.cpu().numpy()).all()
