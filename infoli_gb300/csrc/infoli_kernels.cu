@@ -540,7 +540,10 @@ __global__ void __launch_bounds__(BLOCK, 1) step_kernel(const __grid_constant__ 
   // stamped plans read each receiver's partial slots four at a time: the gaps
   // between receivers' slot blocks must hold zeros (nothing writes them)
   if (LL)
-    for (int i = tid; i < shp.max_slots; i += blockDim.x) part[i] = 0.0f;
+    for (int i = tid; i < shp.max_slots; i += blockDim.x) {
+      part[i] = 0.0f;
+      if (KAHAN) partc[i] = 0.0f;
+    }
   if (tid == 0) {
     mbar_init(&mbar[0], 1);
     mbar_init(&mbar[1], 1);
@@ -684,7 +687,31 @@ __global__ void __launch_bounds__(BLOCK, 1) step_kernel(const __grid_constant__ 
     // ---------------- phase B: voltage step, one thread per owned cell
     if (owner) {
       float ic;
-      if (KAHAN) {
+      if (KAHAN && LL) {
+        // stamped plans: float4 reads of the partial sums and their
+        // compensations (slot blocks 16-byte aligned, zero gaps).  The partials
+        // are added in slot order with an error-free TwoSum per addition, so
+        // the dependent chain is one add per slot; the rounding errors and the
+        // lanes' compensations are summed beside it and applied once.
+        float s = 0.0f, e = 0.0f, c = 0.0f;
+        const float4* p4 = reinterpret_cast<const float4*>(part + slots.x);
+        const float4* c4 = reinterpret_cast<const float4*>(partc + slots.x);
+        const int nq = (slots.y + 3) >> 2;
+        for (int q = 0; q < nq; ++q) {
+          const float4 p = p4[q];
+          const float4 cc = c4[q];
+          c += (cc.x + cc.y) + (cc.z + cc.w);
+          const float pv[4] = {p.x, p.y, p.z, p.w};
+#pragma unroll
+          for (int j = 0; j < 4; ++j) {
+            const float t = s + pv[j];
+            const float bp = t - s;
+            e += (s - (t - bp)) + (pv[j] - bp);
+            s = t;
+          }
+        }
+        ic = s + (e - c);
+      } else if (KAHAN) {
         float s = 0.0f, cmp = 0.0f;
         for (int q = 0; q < slots.y; ++q) {
           const float y = part[slots.x + q] - (partc[slots.x + q] + cmp);

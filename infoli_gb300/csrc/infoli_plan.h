@@ -144,7 +144,8 @@ enum { kGateFloats = 17 };
 //   [tile buffers: nbuf x tile_cap floats]
 //   [cell arrays: kCellArrays x cells_cap floats]
 //   [gate state: cells_cap doubles (Ca2+), kGateFloats x cells_cap floats]
-//   [partial sums: max_slots floats][Kahan compensations: max_slots floats]
+//   [partial sums: max_slots floats][Kahan compensations: max_slots floats,
+//    16-byte aligned]
 //   [2 mbarriers, 16-byte aligned]
 //   resident plans only: [tile descs][chunk descs][per-edge g][edge offsets]
 typedef struct {
@@ -166,6 +167,7 @@ static inline INFOLI_HD SmemLayout smem_layout(SmemShape s) {
   off = (off + 15) & ~(size_t)15;  // stamped plans read partial slots as float4
   L.part = off;
   off += (size_t)s.max_slots * sizeof(float);
+  off = (off + 15) & ~(size_t)15;  // stamped Kahan plans read compensations as float4
   L.partc = off;
   if (s.kahan) off += (size_t)s.max_slots * sizeof(float);
   off = (off + 15) & ~(size_t)15;

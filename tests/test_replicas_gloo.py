@@ -43,4 +43,18 @@ def test_reference_arm_under_two_ranks_prints_one_line(built):
     assert len(lines) == 1  # rank 0 alone prints; rank 1 exits without work
     d = lines[0]
     assert d["impl"] == "reference" and d["n_gpus"] == 2 and d["value"] > 0
-    assert d["e2e"]["h2d_bytes_per_step"] == 0 and d["cpu_baseline"]["kind"] == "port"
+    assert d["e2e"]["h2d_bytes_per_step"] == 0 and d["cpu_baseline"]["kind"] in ("reference", "port")
+
+
+def test_reference_arm_loads_nothing_from_the_product(built):
+    """The reference arm times the reference's own build (or the oracle port)
+    and must not load the GPU library or import the product package."""
+    code = ("import runpy, sys\n"
+            "sys.argv = ['bench.py', '--impl', 'reference', '--steps', '1', '--warmup', '0']\n"
+            "try:\n    runpy.run_path('bench.py', run_name='__main__')\nexcept SystemExit:\n    pass\n"
+            "maps = open('/proc/self/maps').read()\n"
+            "print('PRODUCT', 'infoli_gb300' in sys.modules, 'libinfoli_gpu' in maps)\n")
+    r = subprocess.run([sys.executable, "-c", code], cwd=ROOT, capture_output=True, text=True, timeout=600,
+                       env=dict(os.environ, OMP_NUM_THREADS="2"))
+    assert r.returncode == 0, r.stdout + r.stderr
+    assert "PRODUCT False False" in r.stdout, r.stdout
