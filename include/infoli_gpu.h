@@ -313,7 +313,19 @@ typedef struct {
    * environment variable (512), else 1024.  infoli_batch_autotune picks it
    * by measurement. */
   int block;
+  /* which networks keep their bitmask rows in shared memory for the launch
+   * (the rest stream them from L2/HBM every step):
+   *   INFOLI_RES_FIT  every network whose rows fit in a CTA's shared memory
+   *                   (the default);
+   *   INFOLI_RES_OCC  only those whose rows fit while the CTAs per SM the
+   *                   shape allows stay resident (two 512-thread CTAs per
+   *                   SM; the same as INFOLI_RES_FIT for 1,024 threads);
+   *   INFOLI_RES_NONE none.
+   * infoli_batch_autotune picks it together with block. */
+  int residency;
 } infoli_batch_desc;
+
+enum { INFOLI_RES_FIT = 0, INFOLI_RES_OCC = 1, INFOLI_RES_NONE = 2 };
 
 /* Uploads the batch and packs it into thread-block clusters.  The stimulus
  * defaults to the reference's pulse (6 uA/cm2, steps 20000 to 20498) on every
@@ -338,21 +350,27 @@ int infoli_batch_cta_info(infoli_batch* b, int* max_active_clusters, int32_t* ne
                           int64_t* end_ns);
 int infoli_batch_destroy(infoli_batch* b);
 
-/* Autotuner of the batch's launch shape (no counterpart in the reference).
- * It times each CTA shape (desc->block = 1024, then 512) on a trial batch of
- * a stratified sample of desc's networks (sorted by size, evenly spaced,
- * the fewest networks whose cells fill every SM twice over at 1,024 cells
- * per SM, at most max_sample when max_sample > 0, else at most 4,096), with
- * desc's flags, state and conductances: one run of trial_steps steps to
- * capture the graph, then one timed run.  It returns the faster shape in
- * out->block (1024 on a tie) and the device time per step of each shape;
- * pass out->block as desc->block to infoli_batch_create.  The trial steps start at step 0, so
- * they see no stimulus pulse.  desc itself is not modified. */
+/* Autotuner of the batch's launch layout (no counterpart in the reference).
+ * It times every candidate pair of cells per CTA and bitmask-row residency
+ *   (1024, FIT), (1024, NONE), (512, FIT), (512, OCC), (512, NONE)
+ * on a trial batch of a stratified sample of desc's networks (sorted by
+ * size, evenly spaced, the fewest networks whose cells fill every SM twice
+ * over at 1,024 cells per SM, at most max_sample when max_sample > 0, else at
+ * most 4,096), with desc's flags, state and conductances: one run of
+ * trial_steps steps to capture the graph, then one timed run.  It returns the
+ * fastest pair in out->block and out->residency (the earlier candidate on a
+ * tie) and the device time per step of every candidate; pass both to
+ * infoli_batch_create.  The trial steps start at step 0, so they see no
+ * stimulus pulse.  desc itself is not modified. */
+enum { INFOLI_TUNE_CANDIDATES = 5 };
 typedef struct {
-  int block;            /* the faster shape: 1024 or 512 */
+  int block;            /* the fastest candidate's cells per CTA: 1024 or 512 */
+  int residency;        /* and its INFOLI_RES_* policy */
   int sample_nets;      /* networks in the trial batch */
   int64_t sample_cells; /* their cells */
-  float ms_per_step[2]; /* trial device time per step: [0] block 1024, [1] block 512 */
+  int cand_block[INFOLI_TUNE_CANDIDATES];
+  int cand_residency[INFOLI_TUNE_CANDIDATES];
+  float cand_ms_per_step[INFOLI_TUNE_CANDIDATES];  /* trial device time per step */
 } infoli_batch_tune;
 int infoli_batch_autotune(const infoli_batch_desc* desc, int max_sample, int trial_steps, infoli_batch_tune* out);
 /* The autotuner's sample (host only, no GPU): writes the indices of the

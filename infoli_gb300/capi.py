@@ -86,15 +86,24 @@ class BatchDesc(C.Structure):
         ("flags", C.c_int),
         ("device", C.c_int),
         ("block", C.c_int),
+        ("residency", C.c_int),
     ]
+
+
+RES_FIT, RES_OCC, RES_NONE = 0, 1, 2
+RES_NAMES = {RES_FIT: "fit", RES_OCC: "occupancy", RES_NONE: "none"}
+TUNE_CANDIDATES = 5
 
 
 class BatchTune(C.Structure):
     _fields_ = [
         ("block", C.c_int),
+        ("residency", C.c_int),
         ("sample_nets", C.c_int),
         ("sample_cells", C.c_int64),
-        ("ms_per_step", C.c_float * 2),
+        ("cand_block", C.c_int * TUNE_CANDIDATES),
+        ("cand_residency", C.c_int * TUNE_CANDIDATES),
+        ("cand_ms_per_step", C.c_float * TUNE_CANDIDATES),
     ]
 
 
@@ -572,10 +581,12 @@ class Batch:
     (then init_values is broadcast)."""
 
     def __init__(self, params, nets, init_state=None, init_values=None, kahan=False, device=0, shape=0,
-                 tune_steps=200, tune_max_sample=0):
+                 tune_steps=200, tune_max_sample=0, residency=RES_FIT):
         """shape: cells per CTA, 1024 or 512; 0 = the library's default;
-        "auto" = infoli_batch_autotune's pick (timed on a sample of the
-        networks, tune_steps steps per shape), kept in self.tune."""
+        "auto" = infoli_batch_autotune's pick of the shape and the residency
+        together (every candidate timed on a sample of the networks,
+        tune_steps steps each), kept in self.tune.  residency: RES_FIT,
+        RES_OCC or RES_NONE (ignored with shape="auto")."""
         L = load()
         self._L = L
         params = np.ascontiguousarray(params, dtype=np.float32)
@@ -605,11 +616,16 @@ class Batch:
         if shape == "auto":
             t = BatchTune()
             _check(L.infoli_batch_autotune(C.byref(d), int(tune_max_sample), int(tune_steps), C.byref(t)))
-            self.tune = {"block": t.block, "sample_nets": t.sample_nets, "sample_cells": t.sample_cells,
-                         "ms_per_step": {1024: t.ms_per_step[0], 512: t.ms_per_step[1]}}
+            self.tune = {"block": t.block, "residency": RES_NAMES[t.residency], "sample_nets": t.sample_nets,
+                         "sample_cells": t.sample_cells,
+                         "ms_per_step": {f"{t.cand_block[k]}/{RES_NAMES[t.cand_residency[k]]}": t.cand_ms_per_step[k]
+                                         for k in range(TUNE_CANDIDATES)}}
             d.block = t.block
+            d.residency = t.residency
         else:
             d.block = int(shape)
+            d.residency = int(residency)
+        self.residency = int(d.residency)
         h = C.c_void_p()
         _check(L.infoli_batch_create(C.byref(d), C.byref(h)))
         self._h = h

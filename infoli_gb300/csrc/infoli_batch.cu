@@ -440,6 +440,8 @@ extern "C" int infoli_batch_create(const infoli_batch_desc* d, infoli_batch** ou
   std::memcpy(&b->P, d->params, sizeof(ModelParams));
   if (d->block != 0 && d->block != 512 && d->block != 1024)
     return fail(infoli__fail(INFOLI_ERR_ARG, "batch_create: block %d (0, 512 or 1024)", d->block));
+  if (d->residency < INFOLI_RES_FIT || d->residency > INFOLI_RES_NONE)
+    return fail(infoli__fail(INFOLI_ERR_ARG, "batch_create: residency %d (0, 1 or 2)", d->residency));
   if (cudaSetDevice(b->device) != cudaSuccess) return fail(infoli__fail(INFOLI_ERR_CUDA, "cudaSetDevice failed"));
   if (d->block != 0) {
     b->block = d->block;
@@ -475,10 +477,18 @@ extern "C" int infoli_batch_create(const infoli_batch_desc* d, infoli_batch** ou
     for (long long k = 0; k < (long long)n * wpr; ++k) ones += __builtin_popcount(src[k]);
     weight[i] = (double)ones / n + 64.0;
   }
-  int smem_optin = 0, prio_lo = 0, prio_hi = 0;
+  int smem_optin = 0, smem_sm = 0, prio_lo = 0, prio_hi = 0;
   cudaDeviceGetAttribute(&smem_optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, b->device);
+  cudaDeviceGetAttribute(&smem_sm, cudaDevAttrMaxSharedMemoryPerMultiprocessor, b->device);
   cudaDeviceGetStreamPriorityRange(&prio_lo, &prio_hi);
   const size_t budget = (size_t)smem_optin - 1024;
+  // shared memory a group may spend on resident rows: all of a CTA's budget
+  // (FIT), what keeps 2048 / block CTAs on an SM (OCC; the runtime reserves
+  // 1 KB per CTA), or nothing (NONE)
+  const int ctas_per_sm = 2048 / b->block;
+  const size_t occ_budget = std::min(budget, (size_t)smem_sm / (size_t)ctas_per_sm - 1024);
+  const size_t res_budget = d->residency == INFOLI_RES_NONE ? 0
+                            : d->residency == INFOLI_RES_OCC ? occ_budget : budget;
   for (int cs = max_cs; cs >= 1; --cs) {
     std::vector<int> nets;
     for (int i = 0; i < d->n_nets; ++i)
@@ -495,7 +505,7 @@ extern "C" int infoli_batch_create(const infoli_batch_desc* d, infoli_batch** ou
     int res_rows = 0;  // words per resident row (wpr + 2), max over resident networks
     for (int i : nets) {
       const int wr = (d->n_cells[i] + 31) / 32 + 2;
-      if (vbytes + sizeof(uint32_t) * (size_t)wr * b->block <= budget) res_rows = std::max(res_rows, wr);
+      if (vbytes + sizeof(uint32_t) * (size_t)wr * b->block <= res_budget) res_rows = std::max(res_rows, wr);
     }
     g.res_words = res_rows * b->block;
     g.smem = vbytes + sizeof(uint32_t) * (size_t)g.res_words;
@@ -708,8 +718,10 @@ extern "C" int infoli_batch_destroy(infoli_batch* b) {
 }
 
 // ------------------------------------------------------------------ autotuner
-// The launch shape (cells per CTA, and with it the cluster sizes and how many
-// networks share an SM) is picked by timing both shapes on a trial batch.
+// The launch layout -- cells per CTA (and with it the cluster sizes and how
+// many networks share an SM) together with which networks keep their bitmask
+// rows in shared memory (which in turn decides whether two 512-thread CTAs
+// fit on an SM) -- is picked by timing every candidate on a trial batch.
 // The trial batch is a stratified sample of the networks: sorted by size,
 // m evenly spaced picks, m the smallest count whose cells reach the target
 // (every SM's 1,024 threads twice over; m at most 4,096 unless the caller
@@ -811,25 +823,30 @@ extern "C" int infoli_batch_autotune(const infoli_batch_desc* d, int max_sample,
   t.g = gs.data();
   t.init_state = d->init_state ? st.data() : nullptr;
 
-  const int shapes[2] = {1024, 512};
-  float ms[2] = {0.0f, 0.0f};
-  for (int s = 0; s < 2; ++s) {
-    t.block = shapes[s];
+  const int cand_block[INFOLI_TUNE_CANDIDATES] = {1024, 1024, 512, 512, 512};
+  const int cand_res[INFOLI_TUNE_CANDIDATES] = {INFOLI_RES_FIT, INFOLI_RES_NONE, INFOLI_RES_FIT, INFOLI_RES_OCC,
+                                                INFOLI_RES_NONE};
+  int best = 0;
+  for (int s = 0; s < INFOLI_TUNE_CANDIDATES; ++s) {
+    t.block = cand_block[s];
+    t.residency = cand_res[s];
     infoli_batch* b = nullptr;
     int rc = infoli_batch_create(&t, &b);
     if (rc != INFOLI_OK) return rc;
     // the first run captures the graph for trial_steps; the second is timed
     rc = infoli_batch_run(b, trial_steps);
     if (rc == INFOLI_OK) rc = infoli_batch_run(b, trial_steps);
-    ms[s] = b->last_ms;
+    out->cand_block[s] = cand_block[s];
+    out->cand_residency[s] = cand_res[s];
+    out->cand_ms_per_step[s] = b->last_ms / (float)trial_steps;
     batch_release(b);  // keeps the error message of a failed run
     if (rc != INFOLI_OK) return rc;
+    if (out->cand_ms_per_step[s] < out->cand_ms_per_step[best]) best = s;
   }
   infoli__clear_error();
-  out->block = ms[1] < ms[0] ? 512 : 1024;
+  out->block = cand_block[best];
+  out->residency = cand_res[best];
   out->sample_nets = m;
   out->sample_cells = cells;
-  out->ms_per_step[0] = ms[0] / (float)trial_steps;
-  out->ms_per_step[1] = ms[1] / (float)trial_steps;
   return INFOLI_OK;
 }

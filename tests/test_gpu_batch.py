@@ -145,18 +145,20 @@ def test_batch_rejects_bad_input(ig, conf):
 
 
 def test_batch_autotune_picks_the_faster_shape(ig, conf):
-    """infoli_batch_autotune times both CTA shapes on a sample of the networks
-    (on a GB300 every network: they hold fewer cells than the sample target); the
-    batch built with its pick equals the batch built with that shape
-    explicitly, bit for bit, and the oracle."""
+    """infoli_batch_autotune times every (cells per CTA, row residency)
+    candidate on a sample of the networks (on a GB300 every network: they hold
+    fewer cells than the sample target); the batch built with its pick equals
+    the batch built with that layout explicitly, bit for bit, and the oracle;
+    the layout does not change the results."""
     nets, st0, states, csr = _batch_inputs(ig, conf, SIZES, DENS, GS, seed0=31)
     steps = 500
     with ig.Batch(conf, nets, init_state=st0, shape="auto", tune_steps=50) as bt:
         t = bt.tune
         ms = t["ms_per_step"]
-        assert t["block"] in (512, 1024) and ms[512] > 0 and ms[1024] > 0
-        other = 512 if t["block"] == 1024 else 1024
-        assert ms[t["block"]] <= ms[other]
+        assert set(ms) == {"1024/fit", "1024/none", "512/fit", "512/occupancy", "512/none"}
+        assert all(v > 0 for v in ms.values())
+        assert t["block"] in (512, 1024)
+        assert ms[f"{t['block']}/{t['residency']}"] == min(ms.values())
         import torch
 
         sms = torch.cuda.get_device_properties(0).multi_processor_count
@@ -166,9 +168,16 @@ def test_batch_autotune_picks_the_faster_shape(ig, conf):
         bt.run(steps)
         got = bt.get_state()
         offsets = bt.offsets
-    with ig.Batch(conf, nets, init_state=st0, shape=t["block"]) as same:
+    res = {"fit": ig.capi.RES_FIT, "occupancy": ig.capi.RES_OCC, "none": ig.capi.RES_NONE}
+    with ig.Batch(conf, nets, init_state=st0, shape=t["block"], residency=res[t["residency"]]) as same:
         same.run(steps)
         assert np.array_equal(got, same.get_state())
+    # another layout: same arithmetic per network, so the same bits
+    other = ig.capi.RES_NONE if t["residency"] != "none" else ig.capi.RES_FIT
+    with ig.Batch(conf, nets, init_state=st0, shape=512 if t["block"] == 1024 else 1024,
+                  residency=other) as alt:
+        alt.run(steps)
+        assert np.array_equal(got, alt.get_state())
     for i, (n, _, g) in enumerate(nets):
         ref, _ = _oracle(conf, n, states[i], *csr[i], g, steps)
         dvs = np.max(np.abs(got[O.S["V_soma"], offsets[i]:offsets[i + 1]] - ref[O.S["V_soma"]]))
