@@ -815,7 +815,7 @@ def run_gpu_serving(args, world, rank, local, count=SERVE_REQUESTS, warmup=None)
     conf = ig.read_parameters(CONF_PATH)
     arrivals, reqs = serving_requests(conf, count)
     work = np.array([len(r["col"]) * r["n_steps"] for r in reqs], dtype=np.float64)
-    with ig.Server(conf, device=local, kahan=True) as sv:
+    with ig.Server(conf, device=local, kahan=True, lane_sms=args.lane_sms) as sv:
         # warm-up: small requests through the same server
         wu = [sv.submit(n=r["n"], row_ptr=r["row_ptr"], col=r["col"], n_steps=200, g_uniform=0.04,
                         init_state=r["init_state"]) for r in sorted(reqs, key=lambda r: r["n"])[:warmup]]
@@ -867,6 +867,11 @@ def run_gpu_serving(args, world, rank, local, count=SERVE_REQUESTS, warmup=None)
                    "edges": [int(len(r["col"])) for r in reqs],
                    "arrivals_s": [round(float(a), 4) for a in arrivals],
                    "timing": "host wall clock from the first arrival to the last result (serving is end to end)",
+                   "paths": ("no lane: every request runs its own persistent launch" if args.lane_sms < 0 else
+                             "requests of at most 8192 cells with one conductance run in the lane (the batched "
+                             "cluster kernel relaunched every 2000 steps over all of them, joining between "
+                             f"launches); larger ones each run their own persistent launch and leave "
+                             f"{args.lane_sms or 8} SMs to the lane"),
                    "l2": "inputs larger than L2"},
         "latency_s": {"p50": float(np.percentile(lat, 50)), "p99": float(np.percentile(lat, 99)),
                       "max": float(lat.max())},
@@ -880,6 +885,8 @@ def run_gpu_serving(args, world, rank, local, count=SERVE_REQUESTS, warmup=None)
         "e2e": {"value": served, "unit": "sims/s", "h2d_bytes_per_step": int(in_bytes / count),
                 "d2h_bytes_per_step": int(sum(19 * 4 * r["n"] for r in reqs) / count)},
         "placement_per_request": [i["grid"] for i in infos],
+        "lane_per_request": [i["lane"] for i in infos],
+        "lane_launches_per_request": [i["lane_launches"] for i in infos],
         "prepare_s_per_request": [round(i["prepared_s"] - i["prep_start_s"], 3) for i in infos],
         "launch_wait_s_per_request": [round(i["start_s"] - i["prepared_s"], 3) for i in infos],
         "run_s_per_request": [round(i["done_s"] - i["start_s"], 3) for i in infos],
@@ -945,6 +952,9 @@ def main():
     ap.add_argument("--workload", default="all", choices=["all", "grid10k", "batched", "serving"])
     ap.add_argument("--case", choices=CASES, default=None)
     ap.add_argument("--no-kahan", action="store_true", help="headline with the uncompensated coupling sum")
+    ap.add_argument("--lane-sms", type=int, default=0,
+                    help="serving: SMs larger requests leave to the lane of small ones (0 = the library's "
+                         "default, < 0 = no lane)")
     args = ap.parse_args()
     if args.case:
         return run_case(args.case, args.steps or 100)

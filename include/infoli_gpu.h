@@ -385,10 +385,19 @@ int infoli_batch_tune_sample(int n_nets, const int* n_cells, int max_sample, int
 /* No counterpart in the reference (one network per process).  A server
  * admits simulation requests by device-memory budget, builds each one's plan
  * on a pool of host threads, runs admitted requests side by side on the GPU
- * (each on its own stream and its own share of the SMs, chosen from its size)
  * and keeps their state on the device until they finish.  Requests that
- * arrive while others run start as soon as memory and SMs free up.  A
- * request's result does not depend on the other requests. */
+ * arrive while others run start as soon as memory and SMs free up.
+ *   - Small requests (at most 8,192 cells, one conductance, no repeated
+ *     sender in a row) run in the lane: the batched cluster kernel over
+ *     every small request on the device, relaunched every lane_chunk_steps
+ *     steps; a request that arrives joins at the next launch and leaves when
+ *     its steps are done.  The lane uses whatever SMs the other requests
+ *     leave, and at least lane_sms of them.
+ *   - Larger requests each run their own persistent launch on their own
+ *     stream, with a share of the SMs chosen from their size (at most all
+ *     but lane_sms).
+ * A request's result does not depend on the other requests: which path it
+ * takes and its plan depend on the request alone. */
 typedef struct infoli_server infoli_server;
 
 typedef struct {
@@ -403,6 +412,8 @@ typedef struct {
   int age_ms;            /* prepared requests launch shortest estimated work (edges x steps) first;
                             one submitted this long ago goes ahead of them (oldest first); 0 = 10000,
                             < 0 = arrival order */
+  int lane_sms;          /* SMs that larger requests leave to the lane; 0 = 8, < 0 = no lane */
+  int lane_chunk_steps;  /* steps per lane launch (the join interval); 0 = 2000 */
 } infoli_server_desc;
 
 typedef struct {
@@ -429,6 +440,8 @@ typedef struct {
   double submit_s, admit_s, prepared_s, start_s, done_s;
   int status;                 /* INFOLI_OK or the request's error */
   double prep_start_s;        /* a preparation thread took it (admit_s .. prep_start_s: queued for one) */
+  int lane;                   /* 1: ran in the lane (grid = its CTAs per lane launch) */
+  int lane_launches;          /* lane launches it took part in */
 } infoli_request_info;
 
 int infoli_server_create(const infoli_server_desc* desc, infoli_server** out);

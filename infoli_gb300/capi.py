@@ -118,6 +118,8 @@ class ServerDesc(C.Structure):
         ("prep_threads", C.c_int),
         ("flags", C.c_int),
         ("age_ms", C.c_int),
+        ("lane_sms", C.c_int),
+        ("lane_chunk_steps", C.c_int),
     ]
 
 
@@ -152,6 +154,8 @@ class RequestInfo(C.Structure):
         ("done_s", C.c_double),
         ("status", C.c_int),
         ("prep_start_s", C.c_double),
+        ("lane", C.c_int),
+        ("lane_launches", C.c_int),
     ]
 
 
@@ -685,10 +689,12 @@ class Server:
     """Request loop over many simulations on one GPU (infoli_server_* handle)."""
 
     def __init__(self, params, device=0, hbm_budget=0, max_active=0, work_per_cta=0, backfill_ms=0,
-                 prep_threads=0, kahan=False, age_ms=0):
+                 prep_threads=0, kahan=False, age_ms=0, lane_sms=0, lane_chunk_steps=0):
         """age_ms: prepared requests launch shortest estimated work first, except
         those submitted more than age_ms ago (oldest first); 0 = 10 s, < 0 =
-        arrival order."""
+        arrival order.  lane_sms: SMs larger requests leave to the lane of
+        small requests (0 = 8, < 0 = no lane); lane_chunk_steps: steps per
+        lane launch (0 = 2000)."""
         L = load()
         self._L = L
         self.params = np.ascontiguousarray(params, dtype=np.float32)[:NPARAM].copy()
@@ -702,6 +708,8 @@ class Server:
         d.prep_threads = int(prep_threads)
         d.flags = F_KAHAN if kahan else 0
         d.age_ms = int(age_ms)
+        d.lane_sms = int(lane_sms)
+        d.lane_chunk_steps = int(lane_chunk_steps)
         h = C.c_void_p()
         _check(L.infoli_server_create(C.byref(d), C.byref(h)))
         self._h = h

@@ -34,36 +34,21 @@ namespace {
 
 constexpr float kNegLog2eOver100 = -0.014426950408889634f;  // -log2(e)/100
 
-// One CTA slot of a cluster.
-struct alignas(16) BatchCta {
-  int net;           // network, -1: idle slot
-  int rank;          // rank of this CTA inside its network (0 .. ncta-1)
-  int ncta;          // CTAs of the network
-  int rank0;         // cluster rank of the network's first CTA (ranks are contiguous)
-  int cbeg, ncell;   // owned cells [cbeg, cbeg + ncell), network-local
-  int n;             // cells in the network
-  int wpr;           // bitmask words per receiver row, ceil(n / 32)
-  long long cell_base;  // first cell of the network in the concatenated state arrays
-  long long bits_base;  // word w of receiver r at bits[bits_base + w * n + r]
-  float g;           // conductance of every edge of the network
-  int resident;      // rows of the owned receivers kept in shared memory
-  int cl_sync;       // the cluster holds a network of several CTAs: cluster barrier per step
-  int pad0;
-};
+}  // namespace
+}  // namespace infoli
+
+#include "infoli_lane.h"
+
+namespace infoli {
+namespace {
 
 struct BatchArgs {
   ModelParams P;
   const BatchCta* cta;
-  const uint32_t* bits;
-  float* st;         // INFOLI_NSTATE x total SoA (reference order); Ca2+ row unused
-  double* ca;        // Ca2+ concentration per cell, kept in FP64 between launches
-  long long total;   // cells in the batch
   int vcap;          // floats per V buffer in shared memory
   int res_words;     // shared words for resident rows (per CTA)
-  const int* step;   // current step index of the batch (device)
-  int n_steps;
-  int pulse_start, pulse_end;
-  float pulse_amp;
+  const int* step;   // current step index of the batch (device), for CTAs whose step0 < 0
+  int n_steps;       // steps of the launch, for CTAs whose n_steps < 0
   unsigned long long* cta_ns;  // [2 * grid]: globaltimer at start and end of every CTA
 };
 
@@ -166,18 +151,19 @@ __global__ void __launch_bounds__(BLOCK, 1) batch_kernel(const __grid_constant__
   const bool own = w.net >= 0 && tid < w.ncell;
   const int r = w.cbeg + tid;
   const long long gc = w.cell_base + r;
-  const long long T = a.total;
-  const int step0 = *a.step;
+  const long long T = w.T;
+  const int step0 = w.step0 >= 0 ? w.step0 : *a.step;
+  const int n_steps = w.n_steps >= 0 ? w.n_steps : a.n_steps;  // the same in every CTA of a cluster
 
   Volts v{};
   Gates gs{};
   if (own) {
-    const float* s = a.st;
+    const float* s = w.st;
     v.Vd = s[0 * T + gc];
     gs.r = s[1 * T + gc];
     gs.s = s[2 * T + gc];
     gs.q = s[3 * T + gc];
-    gs.Ca = a.ca[gc];
+    gs.Ca = w.ca[gc];
     gs.ICaH = s[5 * T + gc];
     gs.gCaL = s[6 * T + gc];
     v.Vs = s[7 * T + gc];
@@ -196,7 +182,7 @@ __global__ void __launch_bounds__(BLOCK, 1) batch_kernel(const __grid_constant__
   if (w.net >= 0 && w.resident) {
     for (int i = tid; i < (w.wpr + 2) * BLOCK; i += BLOCK) {
       const int ww = i / BLOCK, rr = i % BLOCK;
-      sbits[i] = rr < w.ncell ? a.bits[w.bits_base + (long long)ww * w.n + w.cbeg + rr] : 0u;
+      sbits[i] = rr < w.ncell ? w.bits[(long long)ww * w.n + w.cbeg + rr] : 0u;
     }
   }
   cluster_sync_all();  // every CTA of the cluster is running before peers write into it
@@ -208,7 +194,7 @@ __global__ void __launch_bounds__(BLOCK, 1) batch_kernel(const __grid_constant__
   cluster_sync_all();
 
   const VoltCoef vk = volt_coef(a.P);
-  for (int t = 0; t < a.n_steps; ++t) {
+  for (int t = 0; t < n_steps; ++t) {
     const int step = step0 + t;
     const float* vcur = vbuf + (t & 1) * a.vcap;
     float* vnxt = vbuf + ((t + 1) & 1) * a.vcap;
@@ -219,12 +205,11 @@ __global__ void __launch_bounds__(BLOCK, 1) batch_kernel(const __grid_constant__
       const float vcs = v.Vd * kVScale;
       sum = w.resident ? couple_warp<KAHAN, true>(own, smem_u32(sbits + tid), 4u * BLOCK, nullptr, 0u, w.wpr, vbase,
                                                   vcs)
-                       : couple_warp<KAHAN, false>(own, 0u, 0u, a.bits + w.bits_base + r, (uint32_t)w.n, w.wpr,
-                                                   vbase, vcs);
+                       : couple_warp<KAHAN, false>(own, 0u, 0u, w.bits + r, (uint32_t)w.n, w.wpr, vbase, vcs);
     }
     if (own) {
       const float ic = sum * (w.g * kInvVScale);
-      const float iapp = (step >= a.pulse_start && step < a.pulse_end) ? a.pulse_amp : 0.0f;
+      const float iapp = (step >= w.pulse_start && step < w.pulse_end) ? w.pulse_amp : 0.0f;
       // ---- fused compartment update
       Currents cur;
       run_units(a.P, 0xffu, v, gs, cur);
@@ -241,12 +226,12 @@ __global__ void __launch_bounds__(BLOCK, 1) batch_kernel(const __grid_constant__
   }
 
   if (own) {
-    float* s = a.st;
+    float* s = w.st;
     s[0 * T + gc] = v.Vd;
     s[1 * T + gc] = gs.r;
     s[2 * T + gc] = gs.s;
     s[3 * T + gc] = gs.q;
-    a.ca[gc] = gs.Ca;
+    w.ca[gc] = gs.Ca;
     s[5 * T + gc] = gs.ICaH;
     s[7 * T + gc] = v.Vs;
     s[8 * T + gc] = gs.m;
@@ -530,8 +515,13 @@ extern "C" int infoli_batch_create(const infoli_batch_desc* d, infoli_batch** ou
         w.n = n;
         w.wpr = (n + 31) / 32;
         w.cell_base = b->cell_base[i];
-        w.bits_base = bits_base[i];
+        w.T = 0;  // device pointers and the stride are filled in after the allocation
         w.g = d->g[i];
+        w.n_steps = -1;
+        w.step0 = -1;
+        w.pulse_start = b->pulse_start;
+        w.pulse_end = b->pulse_end;
+        w.pulse_amp = b->pulse_amp;
         w.resident = (w.wpr + 2) * b->block <= g.res_words ? 1 : 0;
         w.cl_sync = cs > 1 ? 1 : 0;
         b->cta.push_back(w);
@@ -572,6 +562,12 @@ extern "C" int infoli_batch_create(const infoli_batch_desc* d, infoli_batch** ou
       cudaMalloc((void**)&b->d_step, sizeof(int)) != cudaSuccess ||
       cudaMalloc((void**)&b->d_cta_ns, sizeof(unsigned long long) * 2 * b->cta.size()) != cudaSuccess)
     return fail(infoli__fail(INFOLI_ERR_NOMEM, "batch_create: device allocation failed"));
+  for (BatchCta& w : b->cta) {
+    w.st = b->d_st;
+    w.ca = b->d_ca;
+    w.bits = b->d_bits + bits_base[w.net];
+    w.T = b->total;
+  }
   if (cudaMemcpy(b->d_cta, b->cta.data(), sizeof(BatchCta) * b->cta.size(), cudaMemcpyHostToDevice) != cudaSuccess ||
       cudaMemcpy(b->d_bits, tb.data(), sizeof(uint32_t) * tb.size(), cudaMemcpyHostToDevice) != cudaSuccess ||
       cudaMemcpy(b->d_st, st.data(), sizeof(float) * st.size(), cudaMemcpyHostToDevice) != cudaSuccess ||
@@ -597,7 +593,14 @@ extern "C" int infoli_batch_set_stimulus_pulse(infoli_batch* b, int start_step, 
   b->pulse_start = start_step;
   b->pulse_end = end_step;
   b->pulse_amp = amp;
-  b->graph_steps = -1;  // the captured graph holds the old schedule
+  for (BatchCta& w : b->cta) {
+    w.pulse_start = start_step;
+    w.pulse_end = end_step;
+    w.pulse_amp = amp;
+  }
+  BK(cudaSetDevice(b->device));
+  BK(cudaStreamSynchronize(b->stream));
+  BK(cudaMemcpy(b->d_cta, b->cta.data(), sizeof(BatchCta) * b->cta.size(), cudaMemcpyHostToDevice));
   return INFOLI_OK;
 }
 
@@ -615,15 +618,8 @@ extern "C" int infoli_batch_run(infoli_batch* b, int n_steps) {
     BatchArgs a{};
     a.P = b->P;
     a.cta = b->d_cta;
-    a.bits = b->d_bits;
-    a.st = b->d_st;
-    a.ca = b->d_ca;
-    a.total = b->total;
     a.step = b->d_step;
     a.n_steps = n_steps;
-    a.pulse_start = b->pulse_start;
-    a.pulse_end = b->pulse_end;
-    a.pulse_amp = b->pulse_amp;
     a.cta_ns = b->d_cta_ns;
     BK(cudaStreamBeginCapture(b->stream, cudaStreamCaptureModeThreadLocal));
     cudaError_t e = cudaEventRecord(b->fork, b->stream);
@@ -848,5 +844,219 @@ extern "C" int infoli_batch_autotune(const infoli_batch_desc* d, int max_sample,
   out->residency = cand_res[best];
   out->sample_nets = m;
   out->sample_cells = cells;
+  return INFOLI_OK;
+}
+
+// ----------------------------------------------------------------------- lane
+// The serving loop's lane: small networks, each on device buffers of its own,
+// run through the batched kernel in launches of a few thousand steps; between
+// launches networks join and leave.  One launch = one kernel per cluster size
+// (1,024-thread CTAs, one network per cluster), the kernels running
+// concurrently on one stream each, forked from and joined into the lane's
+// stream.  A network's arithmetic does not depend on which others share its
+// launch.
+
+// CTAs one lane launch may hold (the server launches at most one CTA per SM)
+constexpr size_t kLaneTableCtas = 1024;
+
+struct infoli_lane {
+  int device = 0;
+  ModelParams P{};
+  int kahan = 0;
+  size_t budget = 0;  // dynamic shared memory per CTA
+  cudaStream_t stream = nullptr;
+  cudaStream_t gs[8] = {};
+  cudaEvent_t gdone[8] = {};
+  cudaEvent_t fork = nullptr, done = nullptr;
+  BatchCta* h_cta = nullptr;  // pinned: the table of the launch in flight
+  BatchCta* d_cta = nullptr;
+  unsigned long long* d_cta_ns = nullptr;
+  int* d_step = nullptr;
+  size_t cap = 0;  // CTAs the table buffers hold
+  bool launched = false;
+};
+
+int infoli__lane_pack_bits(int n, const int64_t* row_ptr, const int32_t* col, uint32_t* out) {
+  const int wpr = (n + 31) / 32;
+  std::fill(out, out + (size_t)n * (wpr + 2), 0u);
+  for (int r = 0; r < n; ++r)
+    for (int64_t e = row_ptr[r]; e < row_ptr[r + 1]; ++e) {
+      const int s = col[e];
+      if (s < 0 || s >= n) return -1;
+      if (s == r) continue;  // a self edge adds f(0) * 0 = 0
+      uint32_t& x = out[(size_t)(s / 32) * n + r];
+      const uint32_t bit = 1u << (31 - s % 32);
+      if (x & bit) return -2;  // a repeated sender cannot be one bit
+      x |= bit;
+    }
+  return 0;
+}
+
+int infoli__lane_ctas(int n) { return (n + 1023) / 1024; }
+
+void infoli__lane_destroy(infoli_lane* L) {
+  if (!L) return;
+  cudaSetDevice(L->device);
+  if (L->stream) cudaStreamSynchronize(L->stream);
+  if (L->h_cta) cudaFreeHost(L->h_cta);
+  for (void* p : {(void*)L->d_cta, (void*)L->d_cta_ns, (void*)L->d_step})
+    if (p) cudaFree(p);
+  for (int k = 0; k < 8; ++k) {
+    if (L->gdone[k]) cudaEventDestroy(L->gdone[k]);
+    if (L->gs[k]) cudaStreamDestroy(L->gs[k]);
+  }
+  if (L->fork) cudaEventDestroy(L->fork);
+  if (L->done) cudaEventDestroy(L->done);
+  if (L->stream) cudaStreamDestroy(L->stream);
+  delete L;
+}
+
+int infoli__lane_create(int device, const float* params, int kahan, infoli_lane** out) {
+  *out = nullptr;
+  infoli_lane* L = new infoli_lane();
+  L->device = device;
+  std::memcpy(&L->P, params, sizeof(ModelParams));
+  L->kahan = kahan ? 1 : 0;
+  int smem_optin = 0, prio_lo = 0, prio_hi = 0;
+  if (cudaSetDevice(device) != cudaSuccess ||
+      cudaDeviceGetAttribute(&smem_optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, device) != cudaSuccess ||
+      cudaDeviceGetStreamPriorityRange(&prio_lo, &prio_hi) != cudaSuccess) {
+    infoli__lane_destroy(L);
+    return infoli__fail(INFOLI_ERR_CUDA, "lane: no CUDA device %d", device);
+  }
+  L->budget = (size_t)smem_optin - 1024;
+  cudaError_t e = set_attrs(1024, L->budget, 8);
+  if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&L->stream, cudaStreamNonBlocking);
+  for (int k = 0; k < 8 && e == cudaSuccess; ++k) {
+    // larger clusters first (highest priority), as in the batch
+    const int pr = std::max(prio_hi, std::min(prio_lo, prio_hi + (7 - k) * (prio_lo - prio_hi) / 8));
+    e = cudaStreamCreateWithPriority(&L->gs[k], cudaStreamNonBlocking, pr);
+    if (e == cudaSuccess) e = cudaEventCreateWithFlags(&L->gdone[k], cudaEventDisableTiming);
+  }
+  if (e == cudaSuccess) e = cudaEventCreateWithFlags(&L->fork, cudaEventDisableTiming);
+  if (e == cudaSuccess) e = cudaEventCreateWithFlags(&L->done, cudaEventDisableTiming);
+  if (e == cudaSuccess) e = cudaMalloc((void**)&L->d_step, sizeof(int));
+  if (e == cudaSuccess) e = cudaMemset(L->d_step, 0, sizeof(int));
+  // table buffers for kLaneTableCtas CTAs, allocated once: growing them later
+  // would free the old ones, and cudaFree / cudaFreeHost wait for every kernel
+  // on the device
+  if (e == cudaSuccess) e = cudaMallocHost((void**)&L->h_cta, sizeof(BatchCta) * kLaneTableCtas);
+  if (e == cudaSuccess) e = cudaMalloc((void**)&L->d_cta, sizeof(BatchCta) * kLaneTableCtas);
+  if (e == cudaSuccess) e = cudaMalloc((void**)&L->d_cta_ns, sizeof(unsigned long long) * 2 * kLaneTableCtas);
+  if (e == cudaSuccess) L->cap = kLaneTableCtas;
+  if (e != cudaSuccess) {
+    const char* msg = cudaGetErrorString(e);
+    infoli__lane_destroy(L);
+    return infoli__fail(INFOLI_ERR_CUDA, "lane: set-up failed: %s", msg);
+  }
+  *out = L;
+  return INFOLI_OK;
+}
+
+void* infoli__lane_stream(infoli_lane* L) { return L ? (void*)L->stream : nullptr; }
+
+int infoli__lane_query(infoli_lane* L) {
+  if (!L || !L->launched) return 1;
+  const cudaError_t e = cudaEventQuery(L->done);
+  if (e == cudaSuccess) return 1;
+  if (e == cudaErrorNotReady) return 0;
+  return infoli__fail(INFOLI_ERR_CUDA, "lane: %s", cudaGetErrorString(e));
+}
+
+int infoli__lane_launch(infoli_lane* L, const LaneNet* nets, int count) {
+  if (!L || (count > 0 && !nets)) return infoli__fail(INFOLI_ERR_ARG, "lane_launch: bad argument");
+  BK(cudaSetDevice(L->device));
+  if (L->launched) BK(cudaEventSynchronize(L->done));  // the table buffers are reused
+  L->launched = false;
+  size_t total = 0;
+  for (int i = 0; i < count; ++i) {
+    if (nets[i].n <= 0 || nets[i].n > kLaneMaxCells || nets[i].n_steps < 0 || nets[i].step0 < 0)
+      return infoli__fail(INFOLI_ERR_ARG, "lane_launch: network %d (%d cells, %d steps)", i, nets[i].n,
+                          nets[i].n_steps);
+    total += (size_t)infoli__lane_ctas(nets[i].n);
+  }
+  if (total == 0) return INFOLI_OK;
+  if (total > L->cap)
+    return infoli__fail(INFOLI_ERR_CAPACITY, "lane_launch: %zu CTAs (at most %zu per launch)", total, L->cap);
+  struct Grp {
+    int off = 0, grid = 0, vcap = 0, res_words = 0;
+    size_t smem = 0;
+  } grp[8];
+  size_t off = 0;
+  for (int cs = 8; cs >= 1; --cs) {
+    Grp& g = grp[cs - 1];
+    g.off = (int)off;
+    int nmax = 0;
+    for (int i = 0; i < count; ++i)
+      if (infoli__lane_ctas(nets[i].n) == cs) nmax = std::max(nmax, nets[i].n);
+    if (nmax == 0) continue;
+    g.vcap = ((nmax + 31) / 32) * 32 + 32;
+    const size_t vbytes = 2 * sizeof(float) * (size_t)g.vcap;
+    int res_rows = 0;
+    for (int i = 0; i < count; ++i) {
+      const int n = nets[i].n;
+      if (infoli__lane_ctas(n) != cs) continue;
+      const int wr = (n + 31) / 32 + 2;
+      if (vbytes + sizeof(uint32_t) * (size_t)wr * 1024 <= L->budget) res_rows = std::max(res_rows, wr);
+    }
+    g.res_words = res_rows * 1024;
+    g.smem = vbytes + sizeof(uint32_t) * (size_t)g.res_words;
+    for (int i = 0; i < count; ++i) {
+      const LaneNet& q = nets[i];
+      if (infoli__lane_ctas(q.n) != cs) continue;
+      const int per = (q.n + cs - 1) / cs;
+      for (int k = 0; k < cs; ++k) {
+        BatchCta& w = L->h_cta[off++];
+        w = BatchCta{};
+        w.net = i;
+        w.rank = k;
+        w.ncta = cs;
+        w.rank0 = 0;
+        w.cbeg = std::min(q.n, k * per);
+        w.ncell = std::min(q.n, (k + 1) * per) - w.cbeg;
+        w.n = q.n;
+        w.wpr = (q.n + 31) / 32;
+        w.st = q.st;
+        w.ca = q.ca;
+        w.bits = q.bits;
+        w.T = q.n;
+        w.cell_base = 0;
+        w.g = q.g;
+        w.resident = (w.wpr + 2) * 1024 <= g.res_words ? 1 : 0;
+        w.cl_sync = cs > 1 ? 1 : 0;
+        w.n_steps = q.n_steps;
+        w.step0 = q.step0;
+        w.pulse_start = q.pulse_start;
+        w.pulse_end = q.pulse_end;
+        w.pulse_amp = q.pulse_amp;
+      }
+    }
+    g.grid = (int)off - g.off;
+  }
+  BK(cudaMemcpyAsync(L->d_cta, L->h_cta, sizeof(BatchCta) * total, cudaMemcpyHostToDevice, L->stream));
+  BK(cudaEventRecord(L->fork, L->stream));
+  for (int cs = 8; cs >= 1; --cs) {
+    const Grp& g = grp[cs - 1];
+    if (g.grid == 0) continue;
+    BatchArgs a{};
+    a.P = L->P;
+    a.cta = L->d_cta + g.off;
+    a.vcap = g.vcap;
+    a.res_words = g.res_words;
+    a.step = L->d_step;
+    a.n_steps = 0;
+    a.cta_ns = L->d_cta_ns + 2 * (size_t)g.off;
+    cudaLaunchConfig_t cfg;
+    cudaLaunchAttribute at[2];
+    fill_config(cfg, at, g.grid, 1024, cs, g.smem, 0, L->gs[cs - 1]);
+    cfg.numAttrs = 1;  // stream priority comes from the stream
+    BK(cudaStreamWaitEvent(L->gs[cs - 1], L->fork, 0));
+    BK(L->kahan ? cudaLaunchKernelEx(&cfg, batch_kernel<1024, true>, a)
+                : cudaLaunchKernelEx(&cfg, batch_kernel<1024, false>, a));
+    BK(cudaEventRecord(L->gdone[cs - 1], L->gs[cs - 1]));
+    BK(cudaStreamWaitEvent(L->stream, L->gdone[cs - 1], 0));
+  }
+  BK(cudaEventRecord(L->done, L->stream));
+  L->launched = true;
   return INFOLI_OK;
 }

@@ -46,6 +46,14 @@ constexpr size_t kTraceSlotBytes = 64u << 20;
 // device, so creating or destroying one handle would stall the kernels of
 // every other handle; stream-ordered allocation does not.  Freed memory stays
 // in the pool for the next handle (release threshold: unlimited).
+cudaMemPool_t sim_pool(int device);
+
+}  // namespace
+
+extern "C" cudaMemPool_t infoli__device_pool(int device) { return sim_pool(device); }
+
+namespace {
+
 cudaMemPool_t sim_pool(int device) {
   static std::mutex mu;
   static cudaMemPool_t pools[64] = {};
@@ -392,9 +400,12 @@ int infoli_sim_create(const infoli_sim_desc* d, infoli_sim** out) {
     if (make_plan(pin, &wide, &perr) && wide.shape.gather == s->plan.shape.gather) s->plan = std::move(wide);
   }
   if (!planned) return fail(infoli__fail(INFOLI_ERR_ARG, "%s", perr.c_str()));
-  const int cores = max_coresident_ctas(s->plan.threads, s->plan.smem_bytes);
+  cudaError_t occ_err = cudaSuccess;
+  const int cores = max_coresident_ctas(s->plan.threads, s->plan.smem_bytes, &occ_err);
   if (cores < s->plan.grid)
-    return fail(infoli__fail(INFOLI_ERR_CUDA, "plan needs %d co-resident CTAs, device allows %d", s->plan.grid, cores));
+    return fail(infoli__fail(INFOLI_ERR_CUDA, "plan needs %d co-resident CTAs of %d threads and %lld bytes of shared "
+                             "memory, device allows %d (%s)", s->plan.grid, s->plan.threads,
+                             (long long)s->plan.smem_bytes, cores, cudaGetErrorString(occ_err)));
 
   int rc;
   const int dv = s->device;

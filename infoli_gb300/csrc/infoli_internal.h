@@ -21,7 +21,13 @@ unsigned long long infoli__wait_timeout_ns(void);
 #ifdef __cplusplus
 }
 
+#include <cuda_runtime.h>
 #include <nvtx3/nvToolsExt.h>
+
+/* The library's stream-ordered device-memory pool of a device (release
+ * threshold unlimited: freeing into it never unmaps memory, which would wait
+ * for every kernel on the device). */
+extern "C" cudaMemPool_t infoli__device_pool(int device);
 
 /* Named NVTX range for the host phases (plan, upload, run, retire), so a
  * system profiler's timeline shows them; header-only, no library. */

@@ -1507,22 +1507,24 @@ cudaError_t launch_step_kernel(const StepArgs& a, int grid, int threads, cudaStr
   return cudaErrorInvalidValue;
 }
 
-int max_coresident_ctas(int threads, size_t smem) {
+int max_coresident_ctas(int threads, size_t smem, cudaError_t* err) {
   int dev = 0, nsm = 0, per_sm = 0;
-  cudaGetDevice(&dev);
-  cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev);
-  cudaError_t e;
-  if (threads == 1024) {
-    auto fn = step_kernel<1024, false, false, false>;
-    cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-    e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, fn, threads, smem);
-  } else if (threads == 512) {
-    auto fn = step_kernel<512, false, false, false>;
-    cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-    e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, fn, threads, smem);
-  } else {
-    return 0;
+  cudaError_t e = cudaGetDevice(&dev);
+  if (e == cudaSuccess) e = cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev);
+  if (e == cudaSuccess) {
+    if (threads == 1024) {
+      auto fn = step_kernel<1024, false, false, false>;
+      e = cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+      if (e == cudaSuccess) e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, fn, threads, smem);
+    } else if (threads == 512) {
+      auto fn = step_kernel<512, false, false, false>;
+      e = cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+      if (e == cudaSuccess) e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, fn, threads, smem);
+    } else {
+      e = cudaErrorInvalidValue;
+    }
   }
+  if (err) *err = e;
   if (e != cudaSuccess) return 0;
   return per_sm * nsm;
 }

@@ -95,6 +95,6 @@ size_t step_kernel_smem(const StepArgs& a);
 cudaError_t launch_step_kernel(const StepArgs& a, int grid, int threads, cudaStream_t stream);
 
 // Largest co-resident grid for `threads` threads and the given dynamic smem.
-int max_coresident_ctas(int threads, size_t smem);
+int max_coresident_ctas(int threads, size_t smem, cudaError_t* err = nullptr);
 
 }  // namespace infoli

@@ -15,16 +15,24 @@
 //               SMs sized to its work);
 //   running  -> launched on its own stream as soon as its CTAs fit beside the
 //               running simulations (the grids of all running simulations
-//               never exceed the SM count, so every persistent grid is
-//               co-resident and none waits on another); its work overlaps
-//               the others' on the device.  Among prepared requests, those
-//               submitted longer ago than the age limit go first (oldest
-//               first), then the shortest estimated work (edges x steps);
-//               a negative age limit keeps arrival order;
+//               and of the lane's launch in flight never exceed the SM
+//               count, so every persistent grid is co-resident and none
+//               waits on another); its work overlaps the others' on the
+//               device.  Among prepared requests, those submitted longer ago
+//               than the age limit go first (oldest first), then the
+//               shortest estimated work (edges x steps); a negative age
+//               limit keeps arrival order;
 //   done     -> final state copied to the host, device memory released; the
 //               record waits for infoli_server_wait.
-// A request's result does not depend on what runs beside it: its plan and
-// launches depend only on the request itself.
+// Small requests (at most kLaneMaxCells cells, one conductance) take the
+// lane instead: preparation packs their bitmask rows and uploads them with
+// the state to buffers of their own; the scheduler relaunches the batched
+// cluster kernel over all of them every lane_chunk steps, on the SMs the
+// persistent grids leave (at least lane_sms: persistent grids are capped at
+// the SM count minus lane_sms), so a request that arrives while others run
+// joins at the next launch, and one whose steps are done leaves.
+// A request's result does not depend on what runs beside it: its path, plan
+// and arithmetic depend only on the request itself.
 #include <cuda_runtime.h>
 
 #include <algorithm>
@@ -35,11 +43,13 @@
 #include <deque>
 #include <map>
 #include <mutex>
+#include <string>
 #include <thread>
 #include <vector>
 
 #include "../../include/infoli_gpu.h"
 #include "infoli_internal.h"
+#include "infoli_lane.h"
 
 namespace {
 
@@ -67,6 +77,12 @@ struct Request {
   char err[256] = {0};
   infoli_sim* sim = nullptr;
   std::vector<float> result;
+  // the lane
+  bool lane = false;
+  uint32_t* d_bits = nullptr;
+  float* d_st = nullptr;
+  double* d_ca = nullptr;
+  int steps_done = 0, chunk = 0, lane_launches = 0;
 };
 
 }  // namespace
@@ -84,6 +100,14 @@ struct infoli_server {
   std::deque<Request*> to_prep;  // admitted, waiting for a preparation thread
   std::vector<Request*> ready;   // prepared, waiting for SMs
   std::vector<Request*> running;
+  // the lane: prepared small requests, in arrival order; those of the launch
+  // in flight are in lane_run (with lane_nets, which the launch reads)
+  infoli_lane* lane = nullptr;
+  int lane_sms = 8, lane_chunk = 2000, lane_inflight = 0;
+  bool lane_busy = false;
+  std::vector<Request*> lane_reqs;
+  std::vector<Request*> lane_run;
+  std::vector<infoli::LaneNet> lane_nets;
   std::map<int64_t, Request*> all;
   int64_t next_id = 1, completed = 0, mem_in_use = 0;
   int grid_in_use = 0, preparing = 0;
@@ -105,12 +129,68 @@ int64_t estimate_bytes(int64_t n, int64_t edges, bool edge_g) {
   return 2 * entries + (edge_g ? 4 * entries : 0) + entries / 2 + 112 * n + (4 << 20);
 }
 
+// Device bytes of a lane request: bitmask rows (two pad words each), the
+// state, FP64 Ca2+.
+int64_t lane_bytes(int64_t n) { return 4 * n * ((n + 31) / 32 + 2) + 4 * INFOLI_NSTATE * n + 8 * n + (1 << 20); }
+
 // CTAs for a request: enough for one thread per cell, and about one CTA per
-// work_per_cta edge evaluations per step, up to the whole GPU.
+// work_per_cta edge evaluations per step, up to the whole GPU less the SMs
+// left to the lane.
 int grid_for(const infoli_server* sv, int64_t n, int64_t edges) {
   const int64_t by_cells = (n + 1023) / 1024;
   const int64_t by_work = (edges + 64 * n + sv->work_per_cta - 1) / sv->work_per_cta;
-  return (int)std::min<int64_t>(sv->nsm, std::max<int64_t>(1, std::max(by_cells, by_work)));
+  const int64_t cap = sv->lane ? sv->nsm - sv->lane_sms : sv->nsm;
+  return (int)std::min<int64_t>(cap, std::max<int64_t>(1, std::max(by_cells, by_work)));
+}
+
+void lane_free(infoli_server* sv, Request* r) {
+  cudaStream_t s = static_cast<cudaStream_t>(infoli__lane_stream(sv->lane));
+  for (void* p : {(void*)r->d_bits, (void*)r->d_st, (void*)r->d_ca})
+    if (p) cudaFreeAsync(p, s);
+  r->d_bits = nullptr;
+  r->d_st = nullptr;
+  r->d_ca = nullptr;
+}
+
+// Plan-free preparation of a lane request (caller does not hold the lock):
+// bitmask rows and state to device buffers of its own.  Returns 0, -2 when
+// the request cannot take the lane (a repeated sender), or an error status.
+int lane_prepare(infoli_server* sv, Request* r, cudaStream_t s, char* msg, size_t msg_len) {
+  const int n = r->n;
+  std::vector<uint32_t> bits((size_t)n * ((n + 31) / 32 + 2));
+  const int pk = infoli__lane_pack_bits(n, r->row_ptr.data(), r->col.empty() ? nullptr : r->col.data(),
+                                        bits.data());
+  if (pk == -2) return -2;
+  if (pk != 0) {
+    snprintf(msg, msg_len, "request topology: a sender id is outside [0, n_cells)");
+    return INFOLI_ERR_ARG;
+  }
+  std::vector<double> ca((size_t)n);
+  for (int c = 0; c < n; ++c) ca[c] = (double)r->init[(size_t)4 * n + c];
+  // from the library's pool: the default pool would hand freed memory back at
+  // synchronisation points, and unmapping waits for every kernel on the device
+  cudaMemPool_t pool = infoli__device_pool(sv->device);
+  cudaError_t e = pool ? cudaSuccess : cudaErrorMemoryAllocation;
+  if (e == cudaSuccess) e = cudaMallocFromPoolAsync((void**)&r->d_bits, bits.size() * sizeof(uint32_t), pool, s);
+  if (e == cudaSuccess) e = cudaMallocFromPoolAsync((void**)&r->d_st, r->init.size() * sizeof(float), pool, s);
+  if (e == cudaSuccess) e = cudaMallocFromPoolAsync((void**)&r->d_ca, ca.size() * sizeof(double), pool, s);
+  if (e == cudaSuccess)
+    e = cudaMemcpyAsync(r->d_bits, bits.data(), bits.size() * sizeof(uint32_t), cudaMemcpyHostToDevice, s);
+  if (e == cudaSuccess)
+    e = cudaMemcpyAsync(r->d_st, r->init.data(), r->init.size() * sizeof(float), cudaMemcpyHostToDevice, s);
+  if (e == cudaSuccess) e = cudaMemcpyAsync(r->d_ca, ca.data(), ca.size() * sizeof(double), cudaMemcpyHostToDevice, s);
+  if (e == cudaSuccess) e = cudaStreamSynchronize(s);
+  if (e != cudaSuccess) {
+    snprintf(msg, msg_len, "lane upload: %s", cudaGetErrorString(e));
+    for (void* p : {(void*)r->d_bits, (void*)r->d_st, (void*)r->d_ca})
+      if (p) cudaFreeAsync(p, s);
+    cudaStreamSynchronize(s);
+    r->d_bits = nullptr;
+    r->d_st = nullptr;
+    r->d_ca = nullptr;
+    return INFOLI_ERR_NOMEM;
+  }
+  return INFOLI_OK;
 }
 
 void finish(infoli_server* sv, Request* r, int status, const char* msg) {
@@ -126,16 +206,42 @@ void finish(infoli_server* sv, Request* r, int status, const char* msg) {
 // Preparation threads: plan + upload, outside the lock.
 void prep_loop(infoli_server* sv) {
   cudaSetDevice(sv->device);
+  cudaStream_t up = nullptr;
+  cudaStreamCreateWithFlags(&up, cudaStreamNonBlocking);
   std::unique_lock<std::mutex> lk(sv->m);
   for (;;) {
     sv->cv_prep.wait(lk, [&] { return sv->stop || !sv->to_prep.empty(); });
-    if (sv->stop) return;
+    if (sv->stop) break;
     Request* r = sv->to_prep.front();
     sv->to_prep.pop_front();
     ++sv->preparing;
     r->prep_start_s = sv->now();
     lk.unlock();
     InfoliRange nvtx_range("infoli_server_prepare");
+    if (r->lane) {
+      char lmsg[256] = {0};
+      const int lrc = lane_prepare(sv, r, up, lmsg, sizeof lmsg);
+      if (lrc != -2) {
+        std::vector<int64_t>().swap(r->row_ptr);
+        std::vector<int32_t>().swap(r->col);
+        std::vector<float>().swap(r->init);
+        lk.lock();
+        --sv->preparing;
+        if (lrc != INFOLI_OK) {
+          sv->mem_in_use -= r->est_bytes;
+          finish(sv, r, lrc, lmsg);
+        } else {
+          r->dev_bytes = r->est_bytes;
+          r->phase = 2;
+          r->prepared_s = sv->now();
+          sv->lane_reqs.push_back(r);
+        }
+        sv->cv_sched.notify_all();
+        continue;
+      }
+      r->lane = false;  // a repeated sender: the persistent path sums it as given
+      r->grid = grid_for(sv, r->n, (int64_t)r->col.size());
+    }
     infoli_sim_desc d;
     std::memset(&d, 0, sizeof d);
     d.n_cells = r->n;
@@ -178,6 +284,92 @@ void prep_loop(infoli_server* sv) {
     }
     sv->cv_sched.notify_all();
   }
+  lk.unlock();
+  if (up) cudaStreamDestroy(up);
+}
+
+// The lane's launch in flight has finished (or failed): advance its
+// requests, retire those that are done.  Caller holds the lock.
+void lane_complete(infoli_server* sv, std::unique_lock<std::mutex>& lk, int q) {
+  std::vector<Request*> done;
+  for (Request* r : sv->lane_run) {
+    if (q > 0) r->steps_done += r->chunk;
+    ++r->lane_launches;
+    if (q < 0 || r->steps_done >= r->n_steps) done.push_back(r);
+  }
+  sv->lane_run.clear();
+  sv->lane_nets.clear();
+  sv->lane_busy = false;
+  sv->lane_inflight = 0;
+  if (done.empty()) return;
+  char qmsg[256] = {0};
+  if (q < 0) snprintf(qmsg, sizeof qmsg, "%s", infoli_last_error());
+  for (Request* r : done) sv->lane_reqs.erase(std::find(sv->lane_reqs.begin(), sv->lane_reqs.end(), r));
+  lk.unlock();
+  cudaStream_t s = static_cast<cudaStream_t>(infoli__lane_stream(sv->lane));
+  std::vector<int> rcs(done.size(), q < 0 ? q : INFOLI_OK);
+  for (size_t k = 0; k < done.size() && q >= 0; ++k) {
+    Request* r = done[k];
+    const int n = r->n;
+    r->result.resize((size_t)INFOLI_NSTATE * n);
+    std::vector<double> ca((size_t)n);
+    cudaError_t e = cudaMemcpyAsync(r->result.data(), r->d_st, r->result.size() * sizeof(float),
+                                    cudaMemcpyDeviceToHost, s);
+    if (e == cudaSuccess) e = cudaMemcpyAsync(ca.data(), r->d_ca, ca.size() * sizeof(double), cudaMemcpyDeviceToHost, s);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(s);
+    if (e != cudaSuccess) {
+      rcs[k] = INFOLI_ERR_CUDA;
+      snprintf(qmsg, sizeof qmsg, "lane read-back: %s", cudaGetErrorString(e));
+    } else {
+      for (int c = 0; c < n; ++c) r->result[(size_t)4 * n + c] = (float)ca[c];
+    }
+  }
+  for (Request* r : done) lane_free(sv, r);
+  lk.lock();
+  for (size_t k = 0; k < done.size(); ++k) {
+    sv->mem_in_use -= done[k]->est_bytes;
+    finish(sv, done[k], rcs[k], rcs[k] == INFOLI_OK ? nullptr : qmsg);
+  }
+}
+
+// Launch the lane over the prepared small requests that fit on the SMs the
+// persistent grids leave (earliest prepared first; the others wait for the
+// next launch with their state on the device).  Caller holds the lock.
+bool lane_start(infoli_server* sv, std::unique_lock<std::mutex>& lk) {
+  if (sv->lane_busy || sv->lane_reqs.empty()) return false;
+  const int cap = sv->nsm - sv->grid_in_use;
+  int used = 0;
+  for (Request* r : sv->lane_reqs) {
+    const int c = infoli__lane_ctas(r->n);
+    if (used + c > cap) continue;
+    used += c;
+    r->chunk = std::min(sv->lane_chunk, r->n_steps - r->steps_done);
+    if (r->phase != 3) {
+      r->phase = 3;
+      r->start_s = sv->now();
+    }
+    sv->lane_run.push_back(r);
+    infoli::LaneNet q{};
+    q.st = r->d_st;
+    q.ca = r->d_ca;
+    q.bits = r->d_bits;
+    q.n = r->n;
+    q.g = r->g_uniform;
+    q.step0 = r->steps_done;
+    q.n_steps = r->chunk;
+    q.pulse_start = r->pulse_start;
+    q.pulse_end = r->pulse_end;
+    q.pulse_amp = r->pulse_amp;
+    sv->lane_nets.push_back(q);
+  }
+  if (sv->lane_run.empty()) return false;
+  sv->lane_busy = true;
+  sv->lane_inflight = used;
+  lk.unlock();
+  const int rc = infoli__lane_launch(sv->lane, sv->lane_nets.data(), (int)sv->lane_nets.size());
+  lk.lock();
+  if (rc != INFOLI_OK) lane_complete(sv, lk, rc);
+  return true;
 }
 
 // Scheduler: admission, launches, retirement.
@@ -216,11 +408,22 @@ void sched_loop(infoli_server* sv) {
         ++i;
       }
     }
+    // the lane's launch in flight
+    if (sv->lane_busy) {
+      lk.unlock();
+      const int q = infoli__lane_query(sv->lane);
+      lk.lock();
+      if (q != 0) {
+        lane_complete(sv, lk, q);
+        progress = true;
+      }
+    }
     // admit by HBM budget, first in first out with bounded backfill
     const double t = sv->now();
     for (auto it = sv->queue.begin(); it != sv->queue.end();) {
       Request* r = *it;
-      const int admitted_or_running = (int)(sv->running.size() + sv->ready.size() + sv->to_prep.size()) + sv->preparing;
+      const int admitted_or_running =
+          (int)(sv->running.size() + sv->ready.size() + sv->to_prep.size() + sv->lane_reqs.size()) + sv->preparing;
       if (admitted_or_running >= sv->max_active) break;
       if (sv->mem_in_use + r->est_bytes <= sv->budget) {
         sv->mem_in_use += r->est_bytes;
@@ -245,9 +448,12 @@ void sched_loop(infoli_server* sv) {
         return oa ? a->submit_s < b->submit_s : a->work < b->work;
       });
     }
+    // SMs the lane holds: its launch in flight, and at least lane_sms while it
+    // has requests (so persistent grids never take the whole device from it)
+    const int lane_hold = std::max(sv->lane_inflight, sv->lane_reqs.empty() ? 0 : sv->lane_sms);
     for (size_t i = 0; i < sv->ready.size();) {
       Request* r = sv->ready[i];
-      if (sv->grid_in_use + r->grid > sv->nsm) {
+      if (sv->grid_in_use + lane_hold + r->grid > sv->nsm) {
         ++i;
         continue;
       }
@@ -271,6 +477,8 @@ void sched_loop(infoli_server* sv) {
       }
       progress = true;
     }
+    // the lane, on the SMs the persistent grids leave
+    if (sv->lane && lane_start(sv, lk)) progress = true;
     if (!progress) {
       // poll running simulations every 100 us; wake at once on submissions
       sv->cv_sched.wait_for(lk, std::chrono::microseconds(100));
@@ -297,6 +505,16 @@ extern "C" int infoli_server_create(const infoli_server_desc* d, infoli_server**
   sv->backfill_s = d->backfill_ms > 0 ? d->backfill_ms * 1e-3 : 1.0;
   cudaSetDevice(sv->device);
   cudaDeviceGetAttribute(&sv->nsm, cudaDevAttrMultiProcessorCount, sv->device);
+  if (d->lane_sms >= 0) {
+    sv->lane_sms = d->lane_sms > 0 ? std::min(d->lane_sms, sv->nsm - 1) : std::min(8, sv->nsm - 1);
+    sv->lane_chunk = d->lane_chunk_steps > 0 ? d->lane_chunk_steps : 2000;
+    if (sv->lane_sms < 1 || infoli__lane_create(sv->device, d->params, (d->flags & INFOLI_F_KAHAN) ? 1 : 0,
+                                                &sv->lane) != INFOLI_OK) {
+      const std::string msg = infoli_last_error();
+      delete sv;
+      return infoli__fail(INFOLI_ERR_CUDA, "server_create: %s", msg.c_str());
+    }
+  }
   size_t free_b = 0, total_b = 0;
   cudaMemGetInfo(&free_b, &total_b);
   sv->budget = d->hbm_budget > 0 ? d->hbm_budget : (int64_t)(0.8 * (double)free_b);
@@ -334,9 +552,11 @@ extern "C" int infoli_server_submit(infoli_server* sv, const infoli_request_desc
   r->pulse_end = q->pulse_end;
   r->pulse_amp = q->pulse_amp;
   r->flags = sv->flags;
-  r->est_bytes = estimate_bytes(n, edges, q->g != nullptr);
+  // the lane: small networks with one conductance (path chosen from the request alone)
+  r->lane = sv->lane != nullptr && n <= kLaneMaxCells && q->g == nullptr;
+  r->est_bytes = r->lane ? lane_bytes(n) : estimate_bytes(n, edges, q->g != nullptr);
   r->admit_bytes = r->est_bytes;
-  r->grid = grid_for(sv, n, edges);
+  r->grid = r->lane ? infoli__lane_ctas(n) : grid_for(sv, n, edges);
   // the cell update costs about as much as 100 edge evaluations per cell-step
   r->work = ((double)edges + 100.0 * (double)n) * (double)q->n_steps;
   std::lock_guard<std::mutex> lk(sv->m);
@@ -388,6 +608,8 @@ extern "C" int infoli_server_wait(infoli_server* sv, int64_t id, float* out_stat
     info->start_s = r->start_s;
     info->done_s = r->done_s;
     info->status = r->status;
+    info->lane = r->lane ? 1 : 0;
+    info->lane_launches = r->lane_launches;
   }
   int rc = r->status;
   if (rc == INFOLI_OK && out_state) std::memcpy(out_state, r->result.data(), r->result.size() * sizeof(float));
@@ -402,7 +624,8 @@ extern "C" int infoli_server_status(infoli_server* sv, int* queued, int* active,
   if (!sv) return infoli__fail(INFOLI_ERR_ARG, "null handle");
   std::lock_guard<std::mutex> lk(sv->m);
   if (queued) *queued = (int)sv->queue.size();
-  if (active) *active = (int)(sv->running.size() + sv->ready.size() + sv->to_prep.size()) + sv->preparing;
+  if (active)
+    *active = (int)(sv->running.size() + sv->ready.size() + sv->to_prep.size() + sv->lane_reqs.size()) + sv->preparing;
   if (completed) *completed = sv->completed;
   if (hbm_in_use) *hbm_in_use = sv->mem_in_use;
   return INFOLI_OK;
@@ -420,14 +643,17 @@ extern "C" int infoli_server_destroy(infoli_server* sv) {
   if (sv->sched.joinable()) sv->sched.join();
   for (std::thread& t : sv->prep)
     if (t.joinable()) t.join();
+  if (sv->lane) cudaStreamSynchronize(static_cast<cudaStream_t>(infoli__lane_stream(sv->lane)));
   for (auto& kv : sv->all) {
     Request* r = kv.second;
     if (r->sim) {
       infoli_sim_sync(r->sim);
       infoli_sim_destroy(r->sim);
     }
+    if (sv->lane) lane_free(sv, r);
     delete r;
   }
+  infoli__lane_destroy(sv->lane);
   delete sv;
   return INFOLI_OK;
 }
