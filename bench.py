@@ -868,10 +868,10 @@ def run_gpu_serving(args, world, rank, local, count=SERVE_REQUESTS, warmup=None)
                    "arrivals_s": [round(float(a), 4) for a in arrivals],
                    "timing": "host wall clock from the first arrival to the last result (serving is end to end)",
                    "paths": ("no lane: every request runs its own persistent launch" if args.lane_sms < 0 else
-                             "requests of at most 8192 cells with one conductance run in the lane (the batched "
-                             "cluster kernel relaunched every 2000 steps over all of them, joining between "
-                             f"launches); larger ones each run their own persistent launch and leave "
-                             f"{args.lane_sms or 8} SMs to the lane"),
+                             "requests of at most 8192 cells with one conductance and at most 24576 edges per "
+                             "CTA of their cluster run in the lane (the batched cluster kernel relaunched every "
+                             "2000 steps over all of them, joining between launches); the others each run their "
+                             f"own persistent launch, leaving {args.lane_sms} SMs to the lane"),
                    "l2": "inputs larger than L2"},
         "latency_s": {"p50": float(np.percentile(lat, 50)), "p99": float(np.percentile(lat, 99)),
                       "max": float(lat.max())},

@@ -387,13 +387,16 @@ int infoli_batch_tune_sample(int n_nets, const int* n_cells, int max_sample, int
  * on a pool of host threads, runs admitted requests side by side on the GPU
  * and keeps their state on the device until they finish.  Requests that
  * arrive while others run start as soon as memory and SMs free up.
- *   - Small requests (at most 8,192 cells, one conductance, no repeated
- *     sender in a row) run in the lane: the batched cluster kernel over
- *     every small request on the device, relaunched every lane_chunk_steps
- *     steps; a request that arrives joins at the next launch and leaves when
- *     its steps are done.  The lane uses whatever SMs the other requests
- *     leave, and at least lane_sms of them.
- *   - Larger requests each run their own persistent launch on their own
+ *   - Small, light requests (at most 8,192 cells, one conductance, no
+ *     repeated sender in a row, at most lane_edges_per_cta edges per CTA of
+ *     their cluster) run in the lane: the batched cluster kernel over every
+ *     such request on the device, relaunched every lane_chunk_steps steps; a
+ *     request that arrives joins at the next launch and leaves when its
+ *     steps are done.  A lane request runs on its own cluster of one CTA per
+ *     1,024 cells, so only requests whose step that cluster keeps short take
+ *     it.  The lane uses the SMs the other requests leave, and at least
+ *     lane_sms of them.
+ *   - Other requests each run their own persistent launch on their own
  *     stream, with a share of the SMs chosen from their size (at most all
  *     but lane_sms).
  * A request's result does not depend on the other requests: which path it
@@ -412,8 +415,10 @@ typedef struct {
   int age_ms;            /* prepared requests launch shortest estimated work (edges x steps) first;
                             one submitted this long ago goes ahead of them (oldest first); 0 = 10000,
                             < 0 = arrival order */
-  int lane_sms;          /* SMs that larger requests leave to the lane; 0 = 8, < 0 = no lane */
+  int lane_sms;          /* SMs persistent requests leave to the lane; 0 = none kept back, < 0 = no lane */
   int lane_chunk_steps;  /* steps per lane launch (the join interval); 0 = 2000 */
+  int lane_edges_per_cta;  /* lane eligibility: edges per CTA of the request's cluster at most this;
+                              0 = 24576 (about 4 us of a lane step), < 0 = any */
 } infoli_server_desc;
 
 typedef struct {

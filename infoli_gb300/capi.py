@@ -120,6 +120,7 @@ class ServerDesc(C.Structure):
         ("age_ms", C.c_int),
         ("lane_sms", C.c_int),
         ("lane_chunk_steps", C.c_int),
+        ("lane_edges_per_cta", C.c_int),
     ]
 
 
@@ -689,12 +690,13 @@ class Server:
     """Request loop over many simulations on one GPU (infoli_server_* handle)."""
 
     def __init__(self, params, device=0, hbm_budget=0, max_active=0, work_per_cta=0, backfill_ms=0,
-                 prep_threads=0, kahan=False, age_ms=0, lane_sms=0, lane_chunk_steps=0):
+                 prep_threads=0, kahan=False, age_ms=0, lane_sms=0, lane_chunk_steps=0, lane_edges_per_cta=0):
         """age_ms: prepared requests launch shortest estimated work first, except
         those submitted more than age_ms ago (oldest first); 0 = 10 s, < 0 =
-        arrival order.  lane_sms: SMs larger requests leave to the lane of
-        small requests (0 = 8, < 0 = no lane); lane_chunk_steps: steps per
-        lane launch (0 = 2000)."""
+        arrival order.  lane_sms: SMs persistent requests leave to the lane of
+        small requests (0 = none, < 0 = no lane); lane_chunk_steps: steps per
+        lane launch (0 = 2000); lane_edges_per_cta: lane eligibility, edges
+        per CTA of a request's cluster (0 = 24576, < 0 = any)."""
         L = load()
         self._L = L
         self.params = np.ascontiguousarray(params, dtype=np.float32)[:NPARAM].copy()
@@ -710,6 +712,7 @@ class Server:
         d.age_ms = int(age_ms)
         d.lane_sms = int(lane_sms)
         d.lane_chunk_steps = int(lane_chunk_steps)
+        d.lane_edges_per_cta = int(lane_edges_per_cta)
         h = C.c_void_p()
         _check(L.infoli_server_create(C.byref(d), C.byref(h)))
         self._h = h

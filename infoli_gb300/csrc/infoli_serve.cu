@@ -24,12 +24,12 @@
 //               limit keeps arrival order;
 //   done     -> final state copied to the host, device memory released; the
 //               record waits for infoli_server_wait.
-// Small requests (at most kLaneMaxCells cells, one conductance) take the
-// lane instead: preparation packs their bitmask rows and uploads them with
+// Small, light requests (at most kLaneMaxCells cells, one conductance, few
+// edges per CTA of their cluster) take the lane instead: preparation packs their bitmask rows and uploads them with
 // the state to buffers of their own; the scheduler relaunches the batched
 // cluster kernel over all of them every lane_chunk steps, on the SMs the
-// persistent grids leave (at least lane_sms: persistent grids are capped at
-// the SM count minus lane_sms), so a request that arrives while others run
+// persistent grids leave (at least lane_sms when it is set: persistent grids
+// are capped at the SM count minus lane_sms), so a request that arrives while others run
 // joins at the next launch, and one whose steps are done leaves.
 // A request's result does not depend on what runs beside it: its path, plan
 // and arithmetic depend only on the request itself.
@@ -103,7 +103,8 @@ struct infoli_server {
   // the lane: prepared small requests, in arrival order; those of the launch
   // in flight are in lane_run (with lane_nets, which the launch reads)
   infoli_lane* lane = nullptr;
-  int lane_sms = 8, lane_chunk = 2000, lane_inflight = 0;
+  int lane_sms = 0, lane_chunk = 2000, lane_inflight = 0;
+  int64_t lane_edges = 24576;  // < 0: any
   bool lane_busy = false;
   std::vector<Request*> lane_reqs;
   std::vector<Request*> lane_run;
@@ -506,10 +507,10 @@ extern "C" int infoli_server_create(const infoli_server_desc* d, infoli_server**
   cudaSetDevice(sv->device);
   cudaDeviceGetAttribute(&sv->nsm, cudaDevAttrMultiProcessorCount, sv->device);
   if (d->lane_sms >= 0) {
-    sv->lane_sms = d->lane_sms > 0 ? std::min(d->lane_sms, sv->nsm - 1) : std::min(8, sv->nsm - 1);
+    sv->lane_sms = std::min(d->lane_sms, sv->nsm - 1);
     sv->lane_chunk = d->lane_chunk_steps > 0 ? d->lane_chunk_steps : 2000;
-    if (sv->lane_sms < 1 || infoli__lane_create(sv->device, d->params, (d->flags & INFOLI_F_KAHAN) ? 1 : 0,
-                                                &sv->lane) != INFOLI_OK) {
+    sv->lane_edges = d->lane_edges_per_cta > 0 ? d->lane_edges_per_cta : d->lane_edges_per_cta < 0 ? -1 : 24576;
+    if (infoli__lane_create(sv->device, d->params, (d->flags & INFOLI_F_KAHAN) ? 1 : 0, &sv->lane) != INFOLI_OK) {
       const std::string msg = infoli_last_error();
       delete sv;
       return infoli__fail(INFOLI_ERR_CUDA, "server_create: %s", msg.c_str());
@@ -552,8 +553,14 @@ extern "C" int infoli_server_submit(infoli_server* sv, const infoli_request_desc
   r->pulse_end = q->pulse_end;
   r->pulse_amp = q->pulse_amp;
   r->flags = sv->flags;
-  // the lane: small networks with one conductance (path chosen from the request alone)
-  r->lane = sv->lane != nullptr && n <= kLaneMaxCells && q->g == nullptr;
+  // the lane: small, light networks with one conductance (path chosen from the
+  // request alone).  A lane request runs on its own cluster of one CTA per
+  // 1,024 cells; a persistent grid would spread it over more SMs, so only
+  // requests whose lane step stays short take the lane: at most lane_edges
+  // edges per CTA of the cluster (dense small networks measured several
+  // times slower in the lane than on their persistent share).
+  r->lane = sv->lane != nullptr && n <= kLaneMaxCells && q->g == nullptr &&
+            (sv->lane_edges < 0 || edges <= sv->lane_edges * (int64_t)infoli__lane_ctas(n));
   r->est_bytes = r->lane ? lane_bytes(n) : estimate_bytes(n, edges, q->g != nullptr);
   r->admit_bytes = r->est_bytes;
   r->grid = r->lane ? infoli__lane_ctas(n) : grid_for(sv, n, edges);

@@ -53,7 +53,8 @@ def _serve(ig, conf, reqs, **kw):
         return [sv.wait(i) for i in ids]
 
 
-PATHS = {"lane": {}, "persistent": {"lane_sms": -1}}
+# the lane forced for every request of the mix (by default only light ones take it)
+PATHS = {"lane": {"lane_edges_per_cta": -1}, "persistent": {"lane_sms": -1}}
 
 
 @pytest.mark.parametrize("path", list(PATHS))
@@ -131,7 +132,7 @@ def test_requests_join_while_others_run(ig, conf):
     big = dict(n=n_p, row_ptr=rp_p, col=col_p, g=g_p, n_steps=60000, init_state=hetero_state(conf, n_p, 42),
                pulse=(100, 300, 3.0))
     b, c = small(700, 0.2, 600, 43), small(1200, 0.1, 900, 44)
-    with ig.Server(conf, lane_chunk_steps=500) as sv:
+    with ig.Server(conf, lane_chunk_steps=500, lane_edges_per_cta=-1) as sv:
         ia, ip = sv.submit(**a), sv.submit(**big)
         time.sleep(0.05)
         assert sv.poll(ia) == 1 and sv.poll(ip) == 1  # both admitted and on their way
@@ -148,7 +149,7 @@ def test_requests_join_while_others_run(ig, conf):
     assert ia_["lane_launches"] >= 100000 // 500 and ib_["lane_launches"] >= 2
     assert wall > 0
     for req, got in ((a, ra), (b, rb), (c, rc_), (big, rp)):
-        alone = _serve(ig, conf, [req], lane_chunk_steps=500)[0]
+        alone = _serve(ig, conf, [req], lane_chunk_steps=500, lane_edges_per_cta=-1)[0]
         assert np.array_equal(alone[0], got[0]), req["n"]
     for req, got in ((b, rb), (c, rc_)):
         st = req["init_state"].copy()
@@ -164,7 +165,23 @@ def test_lane_join_interval_does_not_change_results(ig, conf):
     rp, col = ig.gen_uniform(1500, 0.1, 51)
     req = dict(n=1500, row_ptr=rp, col=col, n_steps=2100, init_state=hetero_state(conf, 1500, 51),
                pulse=(200, 500, 3.0), g_uniform=0.04)
-    short = _serve(ig, conf, [req], lane_chunk_steps=300)[0]
-    long_ = _serve(ig, conf, [req], lane_chunk_steps=5000)[0]
+    short = _serve(ig, conf, [req], lane_chunk_steps=300, lane_edges_per_cta=-1)[0]
+    long_ = _serve(ig, conf, [req], lane_chunk_steps=5000, lane_edges_per_cta=-1)[0]
     assert short[1]["lane_launches"] == 7 and long_[1]["lane_launches"] == 1
     assert np.array_equal(short[0], long_[0])
+
+
+def test_lane_takes_only_light_requests_by_default(ig, conf):
+    """Default eligibility: a sparse small request takes the lane, a dense one
+    of the same size its own persistent launch (decided from the request
+    alone), each with its alone result."""
+    def req(p, seed):
+        rp, col = ig.gen_uniform(2000, p, seed)
+        return dict(n=2000, row_ptr=rp, col=col, n_steps=400, init_state=hetero_state(conf, 2000, seed),
+                    g_uniform=0.04)
+
+    light, dense = req(0.005, 61), req(0.2, 62)  # ~10 and ~400 senders per cell
+    out = _serve(ig, conf, [light, dense])
+    assert out[0][1]["lane"] == 1 and out[1][1]["lane"] == 0
+    assert np.array_equal(out[0][0], _serve(ig, conf, [light])[0][0])
+    assert np.array_equal(out[1][0], _serve(ig, conf, [dense])[0][0])
