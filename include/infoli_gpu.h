@@ -357,9 +357,11 @@ int infoli_batch_destroy(infoli_batch* b);
  * size, evenly spaced, the fewest networks whose cells fill every SM twice
  * over at 1,024 cells per SM, at most max_sample when max_sample > 0, else at
  * most 4,096), with desc's flags, state and conductances: one run of
- * trial_steps steps to capture the graph, then one timed run.  It returns the
- * fastest pair in out->block and out->residency (the earlier candidate on a
- * tie) and the device time per step of every candidate; pass both to
+ * trial_steps steps to capture the graph, then the best of three timed runs.
+ * It returns the pick in out->block and out->residency -- the first
+ * candidate unless a later one is more than 2% faster than the pick so far
+ * (trial noise is a few percent; the first candidate is the default layout)
+ * -- and the device time per step of every candidate; pass both to
  * infoli_batch_create.  The trial steps start at step 0, so they see no
  * stimulus pulse.  desc itself is not modified. */
 enum { INFOLI_TUNE_CANDIDATES = 5 };

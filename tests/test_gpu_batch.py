@@ -158,7 +158,8 @@ def test_batch_autotune_picks_the_faster_shape(ig, conf):
         assert set(ms) == {"1024/fit", "1024/none", "512/fit", "512/occupancy", "512/none"}
         assert all(v > 0 for v in ms.values())
         assert t["block"] in (512, 1024)
-        assert ms[f"{t['block']}/{t['residency']}"] == min(ms.values())
+        # the pick is within the tuner's 2% margin of the fastest candidate
+        assert ms[f"{t['block']}/{t['residency']}"] * 0.98 <= min(ms.values())
         import torch
 
         sms = torch.cuda.get_device_properties(0).multi_processor_count
