@@ -64,11 +64,12 @@ CONF_PATH = os.path.join(ROOT, "infoli_gb300", "host", "default.conf")
 REF_DIR = os.path.join(ROOT, "oracle", "_ref")
 
 
-def ncu_traffic():
+def ncu_traffic(kahan=True):
     """DRAM bytes (read + write) of one step-kernel launch of this workload, from
-    the committed ncu summary (profiles/step_kernel_grid10k_stamped.md)."""
+    the committed ncu summary of the kernel the headline runs."""
+    name = "step_kernel_grid10k_kahan.md" if kahan else "step_kernel_grid10k_stamped.md"
     try:
-        with open(os.path.join(ROOT, "profiles", "step_kernel_grid10k_stamped.md")) as f:
+        with open(os.path.join(ROOT, "profiles", name)) as f:
             m = re.search(r"traffic \(read \+ write\) per launch \| ([\d,]+) B", f.read())
         return int(m.group(1).replace(",", "")) if m else None
     except OSError:
@@ -513,7 +514,7 @@ def run_gpu(args, world, rank, local):
         "gpu_launches": launches,
         "wall_s": wall,
         "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
-                     "frac": achieved / peak, "traffic": ncu_traffic(),
+                     "frac": achieved / peak, "traffic": ncu_traffic(kahan),
                      "note": f"achieved = algorithmic bytes (132 + N/8 per cell-step) x cells x "
                              f"{STEPS_PER_ITER} timesteps over the step kernel's mean launch time "
                              f"(CUDA events); peak {peak_kind} HBM copy bandwidth; traffic = ncu "
