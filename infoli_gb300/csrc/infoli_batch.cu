@@ -93,6 +93,23 @@ __device__ __forceinline__ void st_peer(float* local, unsigned peer, float v) {
 // receiver pass own == false.
 //   RES: words in shared memory at byte address wsm + 4 * BLOCK * w;
 //   else words in global memory at gw[w * stride].
+// Lockstep iterations per trip of the column walk.
+#ifndef INFOLI_BATCH_UNROLL
+#define INFOLI_BATCH_UNROLL 2
+#endif
+
+// One lockstep iteration: the lane's next set bit of x (leading zeros; 32
+// once x is used up, which reads a pad float and adds nothing), that
+// sender's V_dend x kVScale, its term added to col.
+__device__ __forceinline__ void batch_take(uint32_t& x, uint32_t vcol, float vc, float& col) {
+  const int c = __clz(x);
+  const bool live = x != 0u;
+  x &= __funnelshift_rc(0x7fffffffu, 0u, (unsigned)c);
+  const float V = vc - ld_shared_f32(vcol + 4u * (uint32_t)c);  // scaled by kVScale
+  const float f = fmaf(0.8f, ex2_approx(-(V * V)), 0.2f);
+  if (live) col = fmaf(f, V, col);
+}
+
 template <bool KAHAN, bool RES>
 __device__ __forceinline__ float couple_warp(bool own, uint32_t wsm, uint32_t wstride_b, const uint32_t* gw,
                                             uint32_t stride, int wpr, uint32_t vbase, float vc) {
@@ -118,14 +135,15 @@ __device__ __forceinline__ float couple_warp(bool own, uint32_t wsm, uint32_t ws
     const int m = (int)__reduce_max_sync(0xffffffffu, (unsigned)__popc(x));
     const uint32_t vcol = vbase + 128u * (uint32_t)w;
     float col = 0.0f;  // this column's terms (at most 32)
-    for (int k = 0; k < m; ++k) {
-      const int c = __clz(x);  // 32 once x is used up
-      const bool live = x != 0u;
-      x &= __funnelshift_rc(0x7fffffffu, 0u, (unsigned)c);
-      const float V = vc - ld_shared_f32(vcol + 4u * (uint32_t)c);  // scaled by kVScale
-      const float f = fmaf(0.8f, ex2_approx(-(V * V)), 0.2f);
-      if (live) col = fmaf(f, V, col);
+    // INFOLI_BATCH_UNROLL iterations per trip, then the rest one at a time:
+    // the same terms in the same order either way
+    int k = 0;
+    for (; k + INFOLI_BATCH_UNROLL <= m; k += INFOLI_BATCH_UNROLL) {
+#pragma unroll
+      for (int u = 0; u < INFOLI_BATCH_UNROLL; ++u) batch_take(x, vcol, vc, col);
     }
+#pragma unroll 1
+    for (; k < m; ++k) batch_take(x, vcol, vc, col);
     if (KAHAN) {
       // compensated sum over the column sums
       const float y = col - cmp;
@@ -139,31 +157,39 @@ __device__ __forceinline__ float couple_warp(bool own, uint32_t wsm, uint32_t ws
   return acc;
 }
 
+// BLOCK threads per CTA and 1024 / BLOCK CTAs per SM (64 registers per thread
+// either way).  Only the CTA record's hot fields are held in registers; the
+// state pointers, stride and pulse are read from the record where they are
+// used (the cluster barriers' memory clobbers keep the compiler from holding
+// them across the step loop).
 template <int BLOCK, bool KAHAN>
-__global__ void __launch_bounds__(BLOCK, 1) batch_kernel(const __grid_constant__ BatchArgs a) {
+__global__ void __launch_bounds__(BLOCK, 1024 / BLOCK) batch_kernel(const __grid_constant__ BatchArgs a) {
   extern __shared__ __align__(16) unsigned char smem_raw[];
   float* vbuf = reinterpret_cast<float*>(smem_raw);              // [2][vcap]
   uint32_t* sbits = reinterpret_cast<uint32_t*>(vbuf + 2 * a.vcap);  // [wpr + 2][BLOCK] if resident
   const unsigned long long t_start = globaltimer_ns();
-  const BatchCta w = a.cta[blockIdx.x];
+  const BatchCta* wp = a.cta + blockIdx.x;
+  const int net = wp->net, ncell = wp->ncell, n = wp->n, wpr = wp->wpr;
+  const int ncta = wp->ncta, rank0 = wp->rank0;
+  const bool resident = wp->resident != 0, cl_sync = wp->cl_sync != 0;
   const int tid = threadIdx.x;
   const unsigned me = cluster_rank();
-  const bool own = w.net >= 0 && tid < w.ncell;
-  const int r = w.cbeg + tid;
-  const long long gc = w.cell_base + r;
-  const long long T = w.T;
-  const int step0 = w.step0 >= 0 ? w.step0 : *a.step;
-  const int n_steps = w.n_steps >= 0 ? w.n_steps : a.n_steps;  // the same in every CTA of a cluster
+  const bool own = net >= 0 && tid < ncell;
+  const int r = wp->cbeg + tid;
+  const int step0 = wp->step0 >= 0 ? wp->step0 : *a.step;
+  const int n_steps = wp->n_steps >= 0 ? wp->n_steps : a.n_steps;  // the same in every CTA of a cluster
+  const uint32_t* gbits = wp->bits;
 
   Volts v{};
   Gates gs{};
   if (own) {
-    const float* s = w.st;
+    const long long T = wp->T, gc = wp->cell_base + r;
+    const float* s = wp->st;
     v.Vd = s[0 * T + gc];
     gs.r = s[1 * T + gc];
     gs.s = s[2 * T + gc];
     gs.q = s[3 * T + gc];
-    gs.Ca = w.ca[gc];
+    gs.Ca = wp->ca[gc];
     gs.ICaH = s[5 * T + gc];
     gs.gCaL = s[6 * T + gc];
     v.Vs = s[7 * T + gc];
@@ -179,17 +205,17 @@ __global__ void __launch_bounds__(BLOCK, 1) batch_kernel(const __grid_constant__
     gs.ha = s[17 * T + gc];
     gs.xa = s[18 * T + gc];
   }
-  if (w.net >= 0 && w.resident) {
-    for (int i = tid; i < (w.wpr + 2) * BLOCK; i += BLOCK) {
+  if (net >= 0 && resident) {
+    for (int i = tid; i < (wpr + 2) * BLOCK; i += BLOCK) {
       const int ww = i / BLOCK, rr = i % BLOCK;
-      sbits[i] = rr < w.ncell ? w.bits[(long long)ww * w.n + w.cbeg + rr] : 0u;
+      sbits[i] = rr < ncell ? gbits[(long long)ww * n + wp->cbeg + rr] : 0u;
     }
   }
   cluster_sync_all();  // every CTA of the cluster is running before peers write into it
   if (own) {
     vbuf[r] = v.Vd * kVScale;
-    for (int p = 0; p < w.ncta; ++p)
-      if (w.rank0 + p != (int)me) st_peer(vbuf + r, (unsigned)(w.rank0 + p), v.Vd * kVScale);
+    for (int p = 0; p < ncta; ++p)
+      if (rank0 + p != (int)me) st_peer(vbuf + r, (unsigned)(rank0 + p), v.Vd * kVScale);
   }
   cluster_sync_all();
 
@@ -200,38 +226,38 @@ __global__ void __launch_bounds__(BLOCK, 1) batch_kernel(const __grid_constant__
     float* vnxt = vbuf + ((t + 1) & 1) * a.vcap;
     // ---- coupling: the set bits of the rows (whole warps, owned or not)
     float sum = 0.0f;
-    if (w.net >= 0 && (tid & ~31) < w.ncell) {
+    if (net >= 0 && (tid & ~31) < ncell) {
       const uint32_t vbase = smem_u32(vcur);
       const float vcs = v.Vd * kVScale;
-      sum = w.resident ? couple_warp<KAHAN, true>(own, smem_u32(sbits + tid), 4u * BLOCK, nullptr, 0u, w.wpr, vbase,
-                                                  vcs)
-                       : couple_warp<KAHAN, false>(own, 0u, 0u, w.bits + r, (uint32_t)w.n, w.wpr, vbase, vcs);
+      sum = resident ? couple_warp<KAHAN, true>(own, smem_u32(sbits + tid), 4u * BLOCK, nullptr, 0u, wpr, vbase, vcs)
+                     : couple_warp<KAHAN, false>(own, 0u, 0u, gbits + r, (uint32_t)n, wpr, vbase, vcs);
     }
     if (own) {
-      const float ic = sum * (w.g * kInvVScale);
-      const float iapp = (step >= w.pulse_start && step < w.pulse_end) ? w.pulse_amp : 0.0f;
+      const float ic = sum * (wp->g * kInvVScale);
+      const float iapp = (step >= wp->pulse_start && step < wp->pulse_end) ? wp->pulse_amp : 0.0f;
       // ---- fused compartment update
       Currents cur;
       run_units(a.P, 0xffu, v, gs, cur);
       voltage_step(a.P, vk, v, cur, ic, iapp);
       const float vds = v.Vd * kVScale;
       vnxt[r] = vds;
-      for (int p = 0; p < w.ncta; ++p)
-        if (w.rank0 + p != (int)me) st_peer(vnxt + r, (unsigned)(w.rank0 + p), vds);
+      for (int p = 0; p < ncta; ++p)
+        if (rank0 + p != (int)me) st_peer(vnxt + r, (unsigned)(rank0 + p), vds);
     }
-    if (w.cl_sync)
+    if (cl_sync)
       cluster_sync_all();
     else
       __syncthreads();
   }
 
   if (own) {
-    float* s = w.st;
+    const long long T = wp->T, gc = wp->cell_base + r;
+    float* s = wp->st;
     s[0 * T + gc] = v.Vd;
     s[1 * T + gc] = gs.r;
     s[2 * T + gc] = gs.s;
     s[3 * T + gc] = gs.q;
-    w.ca[gc] = gs.Ca;
+    wp->ca[gc] = gs.Ca;
     s[5 * T + gc] = gs.ICaH;
     s[7 * T + gc] = v.Vs;
     s[8 * T + gc] = gs.m;

@@ -113,6 +113,7 @@ struct infoli_sim {
   int32_t* d_gcol = nullptr;  // gather plans; stamped plans: window sender ids
   int32_t* d_perm = nullptr;  // relabelled plans: caller's cell id of each plan cell
   unsigned long long* d_vll[2] = {nullptr, nullptr};  // stamped exchange words
+  float* d_vds[2] = {nullptr, nullptr};               // bitmask plans: scaled V_dend
   // state
   float* d_vd[2] = {nullptr, nullptr};
   float* d_st = nullptr;
@@ -154,7 +155,7 @@ void release(infoli_sim* s) {
                    s->d_edge_g, s->d_vd[0], s->d_vd[1],  s->d_st,         s->d_ca,
                    s->d_cell_amp, s->d_cell_onset, s->d_bar, s->d_err, s->d_trace[0], s->d_trace[1],
                    s->d_prof, s->d_probes, s->d_vll[0], s->d_vll[1], s->d_gdesc, s->d_stim_table,
-                   s->d_gcol, s->d_perm, s->d_io};
+                   s->d_gcol, s->d_perm, s->d_io, s->d_vds[0], s->d_vds[1]};
   if (s->stream) {
     for (void* p : dptrs)
       if (p) cudaFreeAsync(p, s->stream);
@@ -269,6 +270,8 @@ int fill_args(infoli_sim* s, StepArgs* a) {
   a->prof = s->d_prof;
   a->vll[0] = s->d_vll[0];
   a->vll[1] = s->d_vll[1];
+  a->vds[0] = s->d_vds[0];
+  a->vds[1] = s->d_vds[1];
   a->probes = s->d_probes;
   a->gdesc = reinterpret_cast<const int2*>(s->d_gdesc);
   a->gcol = s->d_gcol;
@@ -442,6 +445,13 @@ int infoli_sim_create(const infoli_sim_desc* d, infoli_sim** out) {
     if (pool_alloc(&s->d_vll[0], np * sizeof(unsigned long long), dv, st0) != cudaSuccess ||
         pool_alloc(&s->d_vll[1], np * sizeof(unsigned long long), dv, st0) != cudaSuccess)
       return fail(infoli__fail(INFOLI_ERR_NOMEM, "sim_create: device allocation failed"));
+  }
+  if (s->plan.shape.gather == 3) {
+    if (pool_alloc(&s->d_vds[0], np * sizeof(float), dv, st0) != cudaSuccess ||
+        pool_alloc(&s->d_vds[1], np * sizeof(float), dv, st0) != cudaSuccess)
+      return fail(infoli__fail(INFOLI_ERR_NOMEM, "sim_create: device allocation failed"));
+    cudaMemsetAsync(s->d_vds[0], 0, np * sizeof(float), st0);
+    cudaMemsetAsync(s->d_vds[1], 0, np * sizeof(float), st0);
   }
 
   std::vector<float> init;

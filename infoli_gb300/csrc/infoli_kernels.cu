@@ -1215,6 +1215,23 @@ __global__ void __launch_bounds__(BLOCK, 1) tgather_kernel(const __grid_constant
 // are compensated with KAHAN; the slices' sums are added in slice order by the
 // receiver's owner thread, which then runs the cell update.  One grid barrier
 // per step.
+// Lockstep iterations per trip of the bitmask walk.
+#ifndef INFOLI_BITS_UNROLL
+#define INFOLI_BITS_UNROLL 2
+#endif
+
+// One lockstep iteration: the lane's next set bit of x (leading zeros; 32
+// once x is used up, which reads the next column's first float and adds
+// nothing), that sender's staged V_dend x kVScale, its term added to col.
+__device__ __forceinline__ void bits_take(uint32_t& x, uint32_t vcol, float vc, float& col) {
+  const int c = __clz(x);
+  const bool live = x != 0u;
+  x &= __funnelshift_rc(0x7fffffffu, 0u, (unsigned)c);
+  const float V = vc - ld_shared_f32(vcol + 4u * (uint32_t)c);  // scaled by kVScale
+  const float f = fmaf(0.8f, ex2_approx(-(V * V)), 0.2f);
+  if (live) col = fmaf(f, V, col);
+}
+
 template <bool KAHAN>
 __device__ __forceinline__ void bits_walk(bool own, const uint32_t* gw, int stride, int cs, int ce, uint32_t vtile,
                                           int c0, float vc, float& acc, float& cmp) {
@@ -1231,14 +1248,15 @@ __device__ __forceinline__ void bits_walk(bool own, const uint32_t* gw, int stri
     const int m = (int)__reduce_max_sync(0xffffffffu, (unsigned)__popc(x));
     const uint32_t vcol = vtile + 128u * (uint32_t)(w - c0);
     float col = 0.0f;
-    for (int k = 0; k < m; ++k) {
-      const int c = __clz(x);  // 32 once x is used up: reads the next column's first float
-      const bool live = x != 0u;
-      x &= __funnelshift_rc(0x7fffffffu, 0u, (unsigned)c);
-      const float V = vc - ld_shared_f32(vcol + 4u * (uint32_t)c);
-      const float f = fmaf(0.8f, ex2_approx((V * V) * kNegLog2eOver100), 0.2f);
-      if (live) col = fmaf(f, V, col);
+    // INFOLI_BITS_UNROLL iterations per trip (less loop control), then the
+    // rest one at a time: the same terms in the same order either way
+    int k = 0;
+    for (; k + INFOLI_BITS_UNROLL <= m; k += INFOLI_BITS_UNROLL) {
+#pragma unroll
+      for (int u = 0; u < INFOLI_BITS_UNROLL; ++u) bits_take(x, vcol, vc, col);
     }
+#pragma unroll 1
+    for (; k < m; ++k) bits_take(x, vcol, vc, col);
     if (KAHAN) {
       const float y = col - cmp;
       const float t2 = acc + y;
@@ -1316,13 +1334,19 @@ __global__ void __launch_bounds__(BLOCK, 1) bits_kernel(const __grid_constant__ 
   const VoltCoef vk = volt_coef(a.P);
   unsigned bar_target = 0, nload = 0;
   int row = 0;
-  __syncthreads();
+  // the staged tiles hold V_dend x kVScale (an edge's exponent is then
+  // -(dV')^2, one multiply less per lockstep iteration): seed this launch's
+  // first step from the state, once, behind one grid barrier; every step
+  // after publishes both copies
+  if (owner) a.vds[a.step0 & 1][cell] = v.Vd * kVScale;
+  bar_target += gridDim.x;
+  if (!grid_sync(a, bar_target, &s_abort, nullptr)) return;
   TraceClock tclock(a.trace_every, a.step0);
   for (int st = 0; st < a.n_steps; ++st) {
     const int step = a.step0 + st;
     const bool trace_now = tclock.take();
-    const float* vcur = a.vd[step & 1];
-    if (owner) sVd[t] = v.Vd;
+    const float* vcur = a.vds[step & 1];
+    if (owner) sVd[t] = v.Vd * kVScale;
     if (w.n_tiles > 0 && tid == 0) {
       fence_proxy_async_global();
       fence_proxy_async_smem();
@@ -1371,7 +1395,7 @@ __global__ void __launch_bounds__(BLOCK, 1) bits_kernel(const __grid_constant__ 
           sum += part[q * R + t];
         }
       }
-      const float ic = sum * a.g_uniform;
+      const float ic = (sum * kInvVScale) * a.g_uniform;  // the sums are in scaled units
       const int ls = step + my_off;
       float iapp;
       if (a.stim_kind == STIM_PULSE)
@@ -1384,6 +1408,7 @@ __global__ void __launch_bounds__(BLOCK, 1) bits_kernel(const __grid_constant__ 
       run_units(a.P, 0xffu, v, g, cur);
       voltage_step(a.P, vk, v, cur, ic, iapp);
       a.vd[(step + 1) & 1][cell] = v.Vd;
+      a.vds[(step + 1) & 1][cell] = v.Vd * kVScale;
       if (trace_now) {
         float* tr = a.trace + (size_t)row * a.trace_nq * np + cell;
         int qi = 0;

@@ -46,6 +46,7 @@ struct StepArgs {
   // state
   float* vd[2];               // V_dend double buffer, V^step in vd[step & 1]
   unsigned long long* vll[2]; // stamped mode: (step << 32 | V_dend bits) per cell, slot step & 1
+  float* vds[2];              // bitmask plans: V_dend x kVScale (the staged tiles), V^step in vds[step & 1]
   const int* probes;          // stamped mode: progress-probe cells (CtaWork::probe_begin..)
   const int2* gdesc;          // stamped mode: {slot, recv} per lane-chunk (32 per group)
   int n_cells;                // cells in the network (stamped words >= n_cells are never written)
