@@ -274,6 +274,17 @@ def run_reference_binary(n, p, sim_ms, threads):
     return n * reference_sim_steps(sim_ms) / t, t
 
 
+def reference_median(n, p, sim_ms, threads, runs=3):
+    """(median cell-steps/s, every run's time in s) of `runs` reference runs, or None."""
+    got = []
+    for _ in range(runs):
+        r = run_reference_binary(n, p, sim_ms, threads)
+        if r is None:
+            return None
+        got.append(r)
+    return statistics.median(x[0] for x in got), [x[1] for x in got]
+
+
 def cpu_port_rate(conf, n, rp, col, st, steps, threads):
     """Oracle restatement of the reference OpenMP loop on the host cores: cell-steps/s."""
     from oracle import oracle as O
@@ -474,14 +485,14 @@ def run_gpu(args, world, rank, local):
     if rank != 0:
         return None
     cpu = None
-    ref = run_reference_binary(n, grid_stand_in_p(), STEPS_PER_ITER * 0.05, threads)
+    ref = reference_median(n, grid_stand_in_p(), STEPS_PER_ITER * 0.05, threads)
     port_rate, port_dt = cpu_port_rate(conf, n, rp, col, st, CPU_SAMPLE_STEPS, threads)
     if ref is not None:
         cpu = {"value": ref[0], "unit": "cell-steps/s", "cores": threads, "cpu": model, "kind": "reference",
-               "sample": f"one run of the untouched reference OpenMP build (gcc -O3 -fopenmp, all host threads) "
-                         f"at the same cell count and mean degree (-n {n} -p {grid_stand_in_p():.6f} -t 50 = "
-                         f"1,000 timesteps, uniform random network), its own execution-time clock: "
-                         f"{ref[1]:.2f} s",
+               "sample": f"the median of three runs of the untouched reference OpenMP build (gcc -O3 -fopenmp, "
+                         f"all host threads) at the same cell count and mean degree (-n {n} -p "
+                         f"{grid_stand_in_p():.6f} -t 50 = 1,000 timesteps, uniform random network), its own "
+                         f"execution-time clock: {', '.join(f'{x:.2f}' for x in ref[1])} s",
                "port": {"value": port_rate, "sample": f"oracle restatement on the grid itself, "
                                                       f"{CPU_SAMPLE_STEPS} timesteps ({port_dt:.1f} s)"}}
     else:
@@ -539,6 +550,111 @@ def run_gpu(args, world, rank, local):
             "ms_per_step": sum(o_ms) / len(o_ms), "steps": len(o_ms),
             "max_abs_dV_soma_mV": o_acc, "clocks": o_clk}
     return result
+
+
+# ------------------------------------------------------- C1 and C3 lines --
+def run_gpu_config(args, world, rank, local, which):
+    """The other single-network configurations, each a sub-object of the
+    default line (one replica per GPU; rank 0's own):
+      c1  1,000 cells, the reference generator at p = 0.1 (seed 1), g = 0.04,
+          the default initial state (all cells alike: the reference's plain
+          run), 20,000 timesteps = 1 s as one bench step; CPU baseline: the
+          reference's own build on exactly this configuration (-n 1000 -p 0.1
+          -t 1000);
+      c3  100,000 cells x 100 senders drawn uniformly, per-edge g U(0.02,
+          0.06), per-cell pulses of amplitude U(0, 8) uA/cm2 at onsets U(0,
+          500) ms lasting 5 ms, 1,000 timesteps per bench step; CPU baseline:
+          the oracle's restatement on the same network (the reference's
+          generator takes minutes at this size and cannot draw per-edge g)."""
+    import numpy as np
+    import torch
+
+    import infoli_gb300 as ig
+    from infoli_gb300 import build
+
+    torch.cuda.set_device(local)
+    build.build()
+    conf = ig.read_parameters(CONF_PATH)
+    g = None
+    stim = None
+    if which == "c1":
+        n, steps_per, iters = 1000, 20000, 3
+        rp, col = ig.gen_uniform(n, 0.1, SEED)
+        st = np.empty((19, n), dtype=np.float32)
+        st[:] = conf[23:42][:, None]
+        name = "1000 cells, reference generator p=0.1 seed=1, g=0.04, default initial state, 20000 timesteps"
+    else:
+        n, steps_per, iters = 100000, 1000, 10
+        rp, col, g = ig.gen_fixed_degree(n, 100, 3, (0.02, 0.06))
+        rng = np.random.default_rng(3)
+        amp = rng.uniform(0.0, 8.0, n).astype(np.float32)
+        onset = rng.integers(0, 10000, n).astype(np.int32)
+        stim = ("cell", amp, onset, 100)
+        from infoli_gb300 import workloads
+
+        st = workloads.perturbed_state(conf, n, np.random.default_rng(3))
+        name = ("100000 cells x 100 uniform senders, g U(0.02,0.06) per edge, per-cell pulses U(0,8) uA/cm2 at "
+                "U(0,500) ms for 5 ms, 1000 timesteps per bench step")
+    sim = ig.Simulation(n, conf, rp, col, g=g, init_state=st, device=local, kahan=True)
+    if stim is not None:
+        sim.set_stimulus_cells(stim[1], stim[2], stim[3])
+    plan = sim.plan_info()
+    warm = min(args.warmup, 3)
+    for _ in range(warm):
+        sim.run(min(steps_per, 1000))
+    sim.set_state(st)
+    dev_ms = []
+    with ClockSampler(local) as clk:
+        for _ in range(iters):
+            flush_l2()
+            sim.run(steps_per)
+            dev_ms.append(sim.last_run_stats()[0])
+    host_state = torch.from_numpy(st).pin_memory().numpy()
+    out_state = torch.empty(st.shape, dtype=torch.float32).pin_memory().numpy()
+    t0 = time.perf_counter()
+    for _ in range(iters):
+        sim.set_state(host_state)
+        sim.run(steps_per)
+        sim.get_state(out=out_state)
+    e2e_s = time.perf_counter() - t0
+    sim.close()
+    if rank != 0:
+        return None
+    threads, model = host_cpu()
+    cell_steps = n * steps_per * iters
+    value = cell_steps / (sum(dev_ms) * 1e-3)
+    if which == "c1":
+        ref = reference_median(n, 0.1, steps_per * 0.05, threads)
+        cpu = None if ref is None else {
+            "value": ref[0], "unit": "cell-steps/s", "cores": threads, "cpu": model, "kind": "reference",
+            "sample": f"the median of three runs of the untouched reference OpenMP build on this configuration "
+                      f"(-n 1000 -p 0.1 -t 1000 = 20,000 timesteps), its own execution-time clock: "
+                      f"{', '.join(f'{x:.2f}' for x in ref[1])} s"}
+    else:
+        cpu = None
+    if cpu is None:
+        from oracle import oracle as O
+
+        s2 = st.copy()
+        ps = 100 if which == "c3" else 2000
+        t0 = time.perf_counter()
+        O.run(n, conf[:23], s2, rp, col, g=g, g_uniform=conf[1], stim=stim, nsteps=ps, trace_every=0, traces=(),
+              nthreads=threads)
+        dt = time.perf_counter() - t0
+        cpu = {"value": n * ps / dt, "unit": "cell-steps/s", "cores": threads, "cpu": model, "kind": "port",
+               "sample": f"the oracle's restatement of the reference loop (C + OpenMP) on the same network, {ps} "
+                         f"timesteps ({dt:.1f} s)"}
+    return {
+        "metric": "cell-steps/s", "value": value, "unit": "cell-steps/s", "steps": iters, "warmup": warm,
+        "ms_per_step": sum(dev_ms) / iters, "higher_is_better": True,
+        "config": {"workload": name, "cells": n, "edges": int(len(col)), "timesteps_per_step": steps_per,
+                   "plan": plan, "kahan": True, "l2": "flushed between timed steps (256 MB memset)"},
+        "e2e": {"value": cell_steps / e2e_s, "unit": "cell-steps/s", "h2d_bytes_per_step": int(st.nbytes),
+                "d2h_bytes_per_step": int(st.nbytes)},
+        "clocks": clk.summary(),
+        "cpu_baseline": cpu,
+        "accuracy": "tests/test_gpu_configs.py checks this configuration against the float oracle at size",
+    }
 
 
 # ---------------------------------------------------------------- batched --
@@ -950,7 +1066,7 @@ def main():
     ap.add_argument("--steps", type=int, default=None)
     ap.add_argument("--warmup", type=int, default=5)
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
-    ap.add_argument("--workload", default="all", choices=["all", "grid10k", "batched", "serving"])
+    ap.add_argument("--workload", default="all", choices=["all", "grid10k", "batched", "serving", "c1", "c3"])
     ap.add_argument("--case", choices=CASES, default=None)
     ap.add_argument("--no-kahan", action="store_true", help="headline with the uncompensated coupling sum")
     ap.add_argument("--lane-sms", type=int, default=0,
@@ -960,7 +1076,8 @@ def main():
     if args.case:
         return run_case(args.case, args.steps or 100)
     if args.steps is None:
-        args.steps = {"all": 20, "grid10k": 20, "batched": 10, "serving": SERVE_REQUESTS}[args.workload]
+        args.steps = {"all": 20, "grid10k": 20, "batched": 10, "serving": SERVE_REQUESTS, "c1": 3, "c3": 10}[
+            args.workload]
     world, rank, local = dist_setup()
     if args.impl == "reference":
         if args.workload == "serving":
@@ -972,6 +1089,12 @@ def main():
         return run_reference(args, world, rank)
     if args.workload == "batched":
         res = run_gpu_batched(args, world, rank, local, warmup=args.warmup)
+        if res is not None:
+            res.update({"n_gpus": world, "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic"})
+            print(json.dumps(res))
+        return 0
+    if args.workload in ("c1", "c3"):
+        res = run_gpu_config(args, world, rank, local, args.workload)
         if res is not None:
             res.update({"n_gpus": world, "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic"})
             print(json.dumps(res))
@@ -988,9 +1111,13 @@ def main():
         # replica per GPU under torchrun: the sub-objects are rank 0's own)
         bres = run_gpu_batched(args, world, rank, local)
         sres = run_gpu_serving(args, world, rank, local)
+        c1 = run_gpu_config(args, world, rank, local, "c1")
+        c3 = run_gpu_config(args, world, rank, local, "c3")
         if line is not None:
             line["batched"] = bres
             line["serving"] = sres
+            line["c1"] = c1
+            line["c3"] = c3
     if line is not None:
         print(json.dumps(line))
     return 0
