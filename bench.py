@@ -1014,7 +1014,7 @@ def run_gpu_serving(args, world, rank, local, count=SERVE_REQUESTS, warmup=None)
 
 
 # ------------------------------------------------------------------ cases --
-CASES = ("grid10k", "uniform1k", "dense10k", "sparse100k", "batch64")
+CASES = ("grid10k", "uniform1k", "dense10k", "sparse100k", "batch64", "serve43k")
 
 
 def run_case(name, steps):
@@ -1023,7 +1023,9 @@ def run_case(name, steps):
       uniform1k  1,000 cells, the reference generator at p = 0.1
       dense10k   10,000 cells, bitmask generator at p = 0.2 (coupling-dominated)
       sparse100k 100,000 cells, 100 senders each, per-edge g U(0.02, 0.06)
-      batch64    the first 64 networks of the batched workload, one graph launch"""
+      batch64    the first 64 networks of the batched workload, one graph launch
+      serve43k   the serving stream's largest request (43,533 cells, density
+                 0.28, g = 0.04), bitmask plan"""
     import numpy as np
 
     import infoli_gb300 as ig
@@ -1041,6 +1043,10 @@ def run_case(name, steps):
     g = None
     if name == "grid10k":
         _, n, rp, col, st = workload()
+    elif name == "serve43k":
+        _, reqs = serving_requests(conf, SERVE_REQUESTS)
+        r = reqs[4]
+        n, rp, col, st = r["n"], r["row_ptr"], r["col"], r["init_state"]
     else:
         if name == "uniform1k":
             n = 1000
