@@ -617,10 +617,21 @@ def run_gpu_config(args, world, rank, local, which):
         sim.run(steps_per)
         sim.get_state(out=out_state)
     e2e_s = time.perf_counter() - t0
+    # accuracy: V_soma every step from the initial state against the FP64
+    # oracle (C3 over fewer steps: the FP64 oracle is slow at 1e7 edges)
+    acc_steps = ACC_STEPS if which == "c1" else 200
+    sim.set_state(st)
+    gpu_soma = sim.run(acc_steps, 1, ig.TRACE_SOMA)["soma"]
     sim.close()
     if rank != 0:
         return None
     threads, model = host_cpu()
+    from oracle import oracle as O
+
+    s64 = np.ascontiguousarray(st, dtype=np.float64)
+    ref64 = O.run(n, np.asarray(conf[:23], dtype=np.float64), s64, rp, col, g=g, g_uniform=conf[1], stim=stim,
+                  nsteps=acc_steps, trace_every=1, traces=("soma",), nthreads=threads, fp64=True)["soma"]
+    acc = float(np.max(np.abs(gpu_soma.astype(np.float64) - ref64)))
     cell_steps = n * steps_per * iters
     value = cell_steps / (sum(dev_ms) * 1e-3)
     if which == "c1":
@@ -653,7 +664,11 @@ def run_gpu_config(args, world, rank, local, which):
                 "d2h_bytes_per_step": int(st.nbytes)},
         "clocks": clk.summary(),
         "cpu_baseline": cpu,
-        "accuracy": "tests/test_gpu_configs.py checks this configuration against the float oracle at size",
+        "accuracy": {"max_abs_dV_soma_mV": acc, "steps": acc_steps, "vs": "FP64 oracle (oracle/, same initial "
+                     "state, topology and stimulus), V_soma every step", "tolerance_mV": ACC_TOL_MV,
+                     "pass": acc <= ACC_TOL_MV,
+                     "at_size": "tests/test_gpu_configs.py checks the configuration against the float oracle over "
+                                "1-2 s of simulated time, spike steps included"},
     }
 
 
