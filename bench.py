@@ -215,16 +215,18 @@ ACC_STEPS = 2000  # window of the accuracy criterion: max |dV_soma| <= 1e-3 mV o
 ACC_TOL_MV = 1e-3
 
 
-def soma_error_vs_fp64(conf, n, rp, col, st, gpu_soma, g_uniform, threads, final_only=False):
+def soma_error_vs_fp64(conf, n, rp, col, st, gpu_soma, g_uniform, threads, final_only=False, step0=0):
     """max |V_soma(GPU) - V_soma(FP64 oracle)| in mV over ACC_STEPS steps from the
-    initial state `st` (every step, or only the state after the last step)."""
+    initial state `st` (every step, or only the state after the last step),
+    the GPU run's first step being step index `step0` (the stimulus schedule
+    depends on it)."""
     import numpy as np
     from oracle import oracle as O
 
     s64 = np.ascontiguousarray(st, dtype=np.float64)
-    ref = O.run(n, np.asarray(conf[:23], dtype=np.float64), s64, rp, col, g_uniform=g_uniform, nsteps=ACC_STEPS,
-                trace_every=0 if final_only else 1, traces=() if final_only else ("soma",), nthreads=threads,
-                fp64=True)
+    ref = O.run(n, np.asarray(conf[:23], dtype=np.float64), s64, rp, col, g_uniform=g_uniform, step0=step0,
+                nsteps=ACC_STEPS, trace_every=0 if final_only else 1, traces=() if final_only else ("soma",),
+                nthreads=threads, fp64=True)
     want = s64[O.S["V_soma"]] if final_only else ref["soma"]
     return float(np.max(np.abs(np.asarray(gpu_soma, dtype=np.float64) - want)))
 
@@ -452,7 +454,9 @@ def run_gpu(args, world, rank, local):
     prof = sim.get_profile()
     sim.set_profiling(False)
     # ---- accuracy: the same initial state, ACC_STEPS steps, V_soma every step
+    # (from the simulation's current step index; the oracle starts there too)
     sim.set_state(st)
+    acc_step0 = sim.step
     gpu_soma = sim.run(ACC_STEPS, 1, ig.TRACE_SOMA)["soma"]
     sim.close()
 
@@ -462,8 +466,9 @@ def run_gpu(args, world, rank, local):
         with ig.Simulation(n, conf, rp, col, init_state=st, device=local, kahan=not kahan) as s2:
             o_ms, o_l, o_clk, _ = time_grid(ig, s2, min(args.steps, 10), min(args.warmup, 3), local, on_row)
             s2.set_state(st)
+            o_step0 = s2.step
             o_soma = s2.run(ACC_STEPS, 1, ig.TRACE_SOMA)["soma"]
-        other = (o_ms, o_clk, o_soma)
+        other = (o_ms, o_clk, o_soma, o_step0)
 
     cell_steps = n * STEPS_PER_ITER * args.steps * world
     value = cell_steps / (total_dev_ms * 1e-3)
@@ -499,7 +504,7 @@ def run_gpu(args, world, rank, local):
         cpu = {"value": port_rate, "unit": "cell-steps/s", "cores": threads, "cpu": model, "kind": "port",
                "sample": f"{CPU_SAMPLE_STEPS} timesteps of the same workload ({port_dt:.1f} s); the reference "
                          f"build could not be made on this host"}
-    acc = soma_error_vs_fp64(conf, n, rp, col, st, gpu_soma, conf[1], threads)
+    acc = soma_error_vs_fp64(conf, n, rp, col, st, gpu_soma, conf[1], threads, step0=acc_step0)
     mode = ("kahan: each lane's two FP32 accumulators are Kahan-compensated (paired f32x2), compensated "
             "partial sums combined per receiver" if kahan else
             "fp32: two FP32 accumulators per lane (paired f32x2), partial sums per receiver in FP32")
@@ -542,8 +547,8 @@ def run_gpu(args, world, rank, local):
         "cpu_baseline": cpu,
     }
     if other is not None:
-        o_ms, o_clk, o_soma = other
-        o_acc = soma_error_vs_fp64(conf, n, rp, col, st, o_soma, conf[1], threads)
+        o_ms, o_clk, o_soma, o_step0 = other
+        o_acc = soma_error_vs_fp64(conf, n, rp, col, st, o_soma, conf[1], threads, step0=o_step0)
         result["precision"]["other_mode"] = {
             "coupling_sum": "fp32" if kahan else "kahan",
             "value": n * STEPS_PER_ITER * len(o_ms) / (sum(o_ms) * 1e-3), "unit": "cell-steps/s",
@@ -620,9 +625,14 @@ def run_gpu_config(args, world, rank, local, which):
     # accuracy: V_soma every step from the initial state against the FP64
     # oracle (C3 over fewer steps: the FP64 oracle is slow at 1e7 edges)
     acc_steps = ACC_STEPS if which == "c1" else 200
-    sim.set_state(st)
-    gpu_soma = sim.run(acc_steps, 1, ig.TRACE_SOMA)["soma"]
     sim.close()
+    # a fresh simulation, so the window is the configuration's first steps
+    # (C3's early pulse onsets fall inside it)
+    with ig.Simulation(n, conf, rp, col, g=g, init_state=st, device=local, kahan=True) as sim:
+        if stim is not None:
+            sim.set_stimulus_cells(stim[1], stim[2], stim[3])
+        acc_step0 = sim.step
+        gpu_soma = sim.run(acc_steps, 1, ig.TRACE_SOMA)["soma"]
     if rank != 0:
         return None
     threads, model = host_cpu()
@@ -630,7 +640,8 @@ def run_gpu_config(args, world, rank, local, which):
 
     s64 = np.ascontiguousarray(st, dtype=np.float64)
     ref64 = O.run(n, np.asarray(conf[:23], dtype=np.float64), s64, rp, col, g=g, g_uniform=conf[1], stim=stim,
-                  nsteps=acc_steps, trace_every=1, traces=("soma",), nthreads=threads, fp64=True)["soma"]
+                  step0=acc_step0, nsteps=acc_steps, trace_every=1, traces=("soma",), nthreads=threads,
+                  fp64=True)["soma"]
     acc = float(np.max(np.abs(gpu_soma.astype(np.float64) - ref64)))
     cell_steps = n * steps_per * iters
     value = cell_steps / (sum(dev_ms) * 1e-3)
