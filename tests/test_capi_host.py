@@ -209,3 +209,8 @@ def test_batch_shape_arguments_rejected_without_crashing(capi):
     with pytest.raises(capi.InfoliError) as e:
         capi.Batch(conf, [(9000, big, 0.04)], init_values=iv, shape="auto")
     assert e.value.code == capi.ERR_ARG
+    # the row-residency policy is FIT, OCC or NONE
+    for bad in (-1, 3):
+        with pytest.raises(capi.InfoliError) as e:
+            capi.Batch(conf, [(100, bits, 0.04)], init_values=iv, shape=1024, residency=bad)
+        assert e.value.code == capi.ERR_ARG
