@@ -253,8 +253,9 @@ def reference_sim_steps(sim_ms):
     return int(np.float32(sim_ms) / np.float32(0.05))
 
 
-def run_reference_binary(n, p, sim_ms, threads):
-    """One run of the untouched reference OpenMP build: -n n -p p -t sim_ms.
+def run_reference_binary(n, p, sim_ms, threads, g=None):
+    """One run of the untouched reference OpenMP build: -n n -p p -t sim_ms
+    (with CONDUCTANCE = g in a copy of its default.conf when g is given).
     Returns (cell-steps/s by its own 'Execution Time for Simulation' clock,
     src/openmp/infoli.c:428,702,721; that time in s)."""
     found = reference_binary()
@@ -264,6 +265,14 @@ def run_reference_binary(n, p, sim_ms, threads):
     env = dict(os.environ, OMP_NUM_THREADS=str(threads))
     d = tempfile.mkdtemp(prefix="infoli_ref_")
     try:
+        if g is not None:
+            # the parameter file is read by position: line 2 is CONDUCTANCE
+            with open(conf) as f:
+                lines = f.read().splitlines()
+            lines[1] = f"CONDUCTANCE = {g:.6f}"
+            conf = os.path.join(d, "default.conf")
+            with open(conf, "w") as f:
+                f.write("\n".join(lines) + "\n")
         r = subprocess.run([exe, "-n", str(n), "-p", f"{p:.6f}", "-t", str(sim_ms), "-c", conf, "-o",
                             os.path.join(d, "out.txt")], capture_output=True, text=True, env=env, cwd=d,
                            timeout=900)
@@ -696,6 +705,20 @@ def batched_workload():
     return conf, nets, st, meta
 
 
+def batched_draws(n_nets=BATCH_NETS, lo=256, hi=8192, dens=(0.05, 0.5), g=(0.02, 0.06), seed=SEED):
+    """The batched workload's per-network sizes, densities and conductances:
+    the first draws of infoli_gb300.workloads.batched (a CPU test checks they
+    agree), restated here so the reference arm loads nothing from the
+    product.  Edge counts are the expected ones."""
+    import numpy as np
+
+    rng = np.random.default_rng(seed)
+    sizes = np.clip(np.exp(rng.uniform(np.log(lo), np.log(hi), n_nets)).astype(np.int64), lo, hi)
+    p = rng.uniform(dens[0], dens[1], n_nets)
+    gs = rng.uniform(g[0], g[1], n_nets).astype(np.float32)
+    return {"sizes": sizes, "density": p, "g": gs, "edges": (sizes * (sizes - 1) * p).astype(np.int64)}
+
+
 def batched_config(meta, extra=None):
     cfg = {
         "workload": f"{BATCH_NETS} independent networks, sizes log-uniform 256-8192, density U(0.05,0.5), "
@@ -737,6 +760,25 @@ def cpu_batched_rate(conf, nets, st, meta, threads, steps=40, k=8):
         t0 = time.perf_counter()
         O.run(n, conf[:23], s, rp, col, g_uniform=g, nsteps=steps, trace_every=0, traces=(), nthreads=threads)
         t_sample += time.perf_counter() - t0
+    est_batch_s = t_sample * (len(nets) / k) * (BATCH_TIMESTEPS / steps)
+    return len(nets) / est_batch_s, t_sample, picks
+
+
+def reference_batched_rate(nets, meta, threads, k=8, sim_ms=5.0):
+    """The reference's own OpenMP build on a stratified sample of the
+    networks, each at its own cell count, density and conductance (its
+    generator draws a uniform random network of that density), sim_ms of
+    simulated time each, timed by its own clock: sims/s (10,000-timestep
+    simulations) extrapolated to the whole batch, or None."""
+    picks = sample_nets(meta, k)
+    t_sample = 0.0
+    for i in picks:
+        r = run_reference_binary(int(meta["sizes"][i]), float(meta["density"][i]), sim_ms, threads,
+                                 g=float(meta["g"][i]))
+        if r is None:
+            return None
+        t_sample += r[1]
+    steps = reference_sim_steps(sim_ms)
     est_batch_s = t_sample * (len(nets) / k) * (BATCH_TIMESTEPS / steps)
     return len(nets) / est_batch_s, t_sample, picks
 
@@ -839,6 +881,18 @@ def run_gpu_batched(args, world, rank, local, warmup=None):
         acc = max(acc, soma_error_vs_fp64(conf, n_i, rp_i, col_i, st[:, off[i]:off[i + 1]], acc_soma[k], g_i,
                                           threads, final_only=True))
     cpu_rate, cpu_t, cpu_picks = cpu_batched_rate(conf, nets, st, meta, threads)
+    ref_b = reference_batched_rate(nets, meta, threads)
+    if ref_b is not None:
+        cpu = {"value": ref_b[0], "unit": "sims/s", "cores": threads, "cpu": model, "kind": "reference",
+               "sample": f"the untouched reference OpenMP build on networks {ref_b[2]} (each -n size -p density, "
+                         f"CONDUCTANCE = its g, -t 5 = 100 timesteps; its own execution-time clock, "
+                         f"{ref_b[1]:.1f} s in all), extrapolated to {len(nets)} networks x {BATCH_TIMESTEPS} "
+                         f"timesteps",
+               "port": {"value": cpu_rate, "sample": f"oracle restatement on networks {cpu_picks} x 40 timesteps "
+                                                     f"({cpu_t:.1f} s), extrapolated"}}
+    else:
+        cpu = {"value": cpu_rate, "unit": "sims/s", "cores": threads, "cpu": model, "kind": "port",
+               "sample": f"networks {cpu_picks} x 40 timesteps ({cpu_t:.1f} s), extrapolated"}
     # algorithmic bytes of one launch: the bitmask rows once per timestep
     # (networks whose rows stay in shared memory are still counted) and 132 B
     # of state per cell-step
@@ -881,8 +935,7 @@ def run_gpu_batched(args, world, rank, local, warmup=None):
                              f"launch time; peak {peak_kind} HBM copy bandwidth; the batched kernel is "
                              f"issue-bound (bit extraction + SFU exp per edge), not HBM-bound"},
         "clocks": clk.summary(),
-        "cpu_baseline": {"value": cpu_rate, "unit": "sims/s", "cores": threads, "cpu": model, "kind": "port",
-                         "sample": f"networks {cpu_picks} x 40 timesteps ({cpu_t:.1f} s), extrapolated"},
+        "cpu_baseline": cpu,
     }
 
 
@@ -892,24 +945,45 @@ def run_reference_batched(args, world, rank):
     from oracle import oracle as O
 
     O.build()
-    conf, nets, st, meta = batched_workload()
+    conf = O.read_parameters(CONF_PATH)
     threads, model = host_cpu()
+    # the networks' sizes, densities and conductances (the same draws as the
+    # GPU arm's workload), without building the bitmasks or loading the product
+    meta = batched_draws()
+    nets = [None] * BATCH_NETS
     rates = []
-    for _ in range(args.warmup):
-        cpu_batched_rate(conf, nets, st, meta, threads, steps=2, k=2)
+    kind = "reference"
+    if reference_batched_rate(nets, meta, threads, k=2) is None:
+        kind = None
     t_total = 0.0
-    for _ in range(args.steps):
-        r, t, picks = cpu_batched_rate(conf, nets, st, meta, threads, steps=5, k=4)
-        rates.append(r)
-        t_total += t
+    picks = []
+    if kind == "reference":
+        for _ in range(args.warmup):
+            reference_batched_rate(nets, meta, threads, k=2)
+        for _ in range(args.steps):
+            r, t, picks = reference_batched_rate(nets, meta, threads, k=4)
+            rates.append(r)
+            t_total += t
+        sample = (f"per bench step the untouched reference OpenMP build on networks {picks} (-n size -p density, "
+                  f"CONDUCTANCE = its g, 100 timesteps, its own clock), extrapolated")
+    else:
+        kind = "port"
+        conf, nets, st, meta = batched_workload()
+        for _ in range(args.warmup):
+            cpu_batched_rate(conf, nets, st, meta, threads, steps=2, k=2)
+        for _ in range(args.steps):
+            r, t, picks = cpu_batched_rate(conf, nets, st, meta, threads, steps=5, k=4)
+            rates.append(r)
+            t_total += t
+        sample = f"per bench step networks {picks} x 5 timesteps of the oracle port, extrapolated"
     value = statistics.mean(rates)
     line = {
         "impl": "reference", "metric": "sims/s", "value": value, "unit": "sims/s (10,000-timestep simulations)",
         "n_gpus": args.gpus, "steps": args.steps, "warmup": args.warmup,
         "ms_per_step": 1e3 * t_total / args.steps, "higher_is_better": True, "scaling": "weak",
         "vs_baseline": None, "dtype": "f32", "data": "synthetic", "config": batched_config(meta),
-        "cpu_baseline": {"value": value, "unit": "sims/s", "cores": threads, "cpu": model, "kind": "port",
-                         "sample": f"per bench step networks {picks} x 5 timesteps, extrapolated"},
+        "cpu_baseline": {"value": value, "unit": "sims/s", "cores": threads, "cpu": model, "kind": kind,
+                         "sample": sample},
         "e2e": {"value": value, "unit": "sims/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
     }
     print(json.dumps(line))

@@ -58,3 +58,21 @@ def test_reference_arm_loads_nothing_from_the_product(built):
                        env=dict(os.environ, OMP_NUM_THREADS="2"))
     assert r.returncode == 0, r.stdout + r.stderr
     assert "PRODUCT False False" in r.stdout, r.stdout
+
+
+def test_reference_arm_batched_draws_match_the_workload():
+    """The batched reference arm draws the networks' sizes, densities and
+    conductances itself (it loads nothing from the product); they are the
+    GPU arm's."""
+    sys.path.insert(0, ROOT)
+    import numpy as np
+
+    import bench
+    import infoli_gb300 as ig
+    from infoli_gb300 import workloads
+
+    conf = ig.read_parameters(bench.CONF_PATH)
+    _, _, meta = workloads.batched(conf, n_nets=40, seed=3)
+    d = bench.batched_draws(n_nets=40, seed=3)
+    assert np.array_equal(d["sizes"], meta["sizes"]) and np.array_equal(d["density"], meta["density"])
+    assert np.array_equal(d["g"], meta["g"])
