@@ -514,8 +514,9 @@ def run_gpu(args, world, rank, local):
                "sample": f"{CPU_SAMPLE_STEPS} timesteps of the same workload ({port_dt:.1f} s); the reference "
                          f"build could not be made on this host"}
     acc = soma_error_vs_fp64(conf, n, rp, col, st, gpu_soma, conf[1], threads, step0=acc_step0)
-    mode = ("kahan: each lane's two FP32 accumulators are Kahan-compensated (paired f32x2), compensated "
-            "partial sums combined per receiver" if kahan else
+    mode = ("kahan: each lane's two FP32 accumulators (paired f32x2) Kahan-add the lane-chunk's terms in "
+            "two-term block sums, the lanes' partial sums and compensations are combined per receiver with "
+            "TwoSum" if kahan else
             "fp32: two FP32 accumulators per lane (paired f32x2), partial sums per receiver in FP32")
     result = {
         "metric": "cell-steps/s", "value": value, "unit": "cell-steps/s", "n_gpus": world,

@@ -192,12 +192,19 @@ using PollBatch = PollBatchT<kPollBatch>;
 // cell and window slot are read again from the window (shared memory) when
 // they are needed.  Measured on the 10k grid: 3.93 against 4.10 us per step
 // (the exchange wait falls by a third, the units slow down under the loads
-// in flight); with Kahan sums the coupling loop loses what the wait gains
-// (4.52 against 4.50 us), so Kahan kernels poll after the units.  Two loads
+// in flight); with Kahan sums the step does not gain (4.52 against 4.50 us
+// with per-term compensation, 4.347 against 4.352 with two-term blocks), so
+// Kahan kernels poll after the units.  Two loads
 // per thread leave part of the window to a second round trip (4.56 us); four
 // spill.
 #ifndef INFOLI_POLL_EARLY
 #define INFOLI_POLL_EARLY 3
+#endif
+// Kahan stamped coupling: compensation over two-term blocks (1, the
+// default) or over every term (0).  Measured on the 10k grid: 4.35 against
+// 4.50 us per step, the same error against the FP64 oracle (4.33e-5 mV).
+#ifndef INFOLI_KAHAN_BLOCK
+#define INFOLI_KAHAN_BLOCK 1
 #endif
 constexpr int kPollEarly = INFOLI_POLL_EARLY;
 
@@ -383,8 +390,11 @@ __device__ __forceinline__ void couple_packed(const unsigned char* sm, const Sme
     return;
   }
   {
-    // Kahan-compensated paired form.  Same sign trick: the accumulators hold
-    // -sum while the compensations c hold +c, so each Kahan step
+    // Kahan-compensated paired form (over two-term blocks by default: each
+    // accumulator's terms of a quad are added first, the block sum is then
+    // Kahan-added, see INFOLI_KAHAN_BLOCK).  Same sign trick: the
+    // accumulators hold -sum while the compensations c hold +c, so each Kahan
+    // step
     //   y = term - c,  s = acc + y,  c = (s - acc) - y,  acc = s
     // becomes, on negated terms nt = -term and nacc = -acc,
     //   ny = fma(f, -V, c),  ns = nacc + ny,  c = ny - (ns - nacc)
@@ -409,20 +419,43 @@ __device__ __forceinline__ void couple_packed(const unsigned char* sm, const Sme
         if (EDGE_G) g4 = gv[qi];
         const unsigned off[4] = {o.x & 0xffffu, o.x >> 16, o.y & 0xffffu, o.y >> 16};
         const float2 gg[2] = {make_float2(g4.x, g4.y), make_float2(g4.z, g4.w)};
+        if (INFOLI_KAHAN_BLOCK) {
+          // the quad's two terms per accumulator are summed first (one
+          // rounding, which the Kahan step after it captures), then
+          // Kahan-added: 6 paired instructions per quad instead of 8
+          float2 nt[2];
 #pragma unroll
-        for (int h = 0; h < 2; ++h) {
-          const float2 x = make_float2(*reinterpret_cast<const float*>(sm + off[2 * h]),
-                                       *reinterpret_cast<const float*>(sm + off[2 * h + 1]));
-          const float2 nv = __fadd2_rn(x, nvc2);  // -V, scaled by kVScale
-          const float2 sq = __fmul2_rn(nv, nv);
-          const float2 e = make_float2(ex2_approx(-sq.x), ex2_approx(-sq.y));
-          float2 f = __ffma2_rn(c08, e, c02);
-          if (EDGE_G) f = __fmul2_rn(gg[h], f);
-          const float2 ny = __ffma2_rn(f, nv, cmp);      // -(term - c)
-          const float2 ns = __fadd2_rn(nacc, ny);        // -(acc + y)
-          const float2 dt = __ffma2_rn(nacc, m1, ns);    // ns - nacc
-          cmp = __ffma2_rn(dt, m1, ny);                  // ny - (ns - nacc) = (s - acc) - y
+          for (int h = 0; h < 2; ++h) {
+            const float2 x = make_float2(*reinterpret_cast<const float*>(sm + off[2 * h]),
+                                         *reinterpret_cast<const float*>(sm + off[2 * h + 1]));
+            const float2 nv = __fadd2_rn(x, nvc2);  // -V, scaled by kVScale
+            const float2 sq = __fmul2_rn(nv, nv);
+            const float2 e = make_float2(ex2_approx(-sq.x), ex2_approx(-sq.y));
+            float2 f = __ffma2_rn(c08, e, c02);
+            if (EDGE_G) f = __fmul2_rn(gg[h], f);
+            nt[h] = h == 0 ? __fmul2_rn(f, nv) : __ffma2_rn(f, nv, nt[0]);  // -(t0 + t2), -(t1 + t3)
+          }
+          const float2 ny = __fadd2_rn(nt[1], cmp);     // -(block - c)
+          const float2 ns = __fadd2_rn(nacc, ny);       // -(acc + y)
+          const float2 dt = __ffma2_rn(nacc, m1, ns);   // ns - nacc
+          cmp = __ffma2_rn(dt, m1, ny);                 // (s - acc) - y
           nacc = ns;
+        } else {
+#pragma unroll
+          for (int h = 0; h < 2; ++h) {
+            const float2 x = make_float2(*reinterpret_cast<const float*>(sm + off[2 * h]),
+                                         *reinterpret_cast<const float*>(sm + off[2 * h + 1]));
+            const float2 nv = __fadd2_rn(x, nvc2);  // -V, scaled by kVScale
+            const float2 sq = __fmul2_rn(nv, nv);
+            const float2 e = make_float2(ex2_approx(-sq.x), ex2_approx(-sq.y));
+            float2 f = __ffma2_rn(c08, e, c02);
+            if (EDGE_G) f = __fmul2_rn(gg[h], f);
+            const float2 ny = __ffma2_rn(f, nv, cmp);      // -(term - c)
+            const float2 ns = __fadd2_rn(nacc, ny);        // -(acc + y)
+            const float2 dt = __ffma2_rn(nacc, m1, ns);    // ns - nacc
+            cmp = __ffma2_rn(dt, m1, ny);                  // ny - (ns - nacc) = (s - acc) - y
+            nacc = ns;
+          }
         }
       }
       // TwoSum of the two accumulators (values un-negated)
