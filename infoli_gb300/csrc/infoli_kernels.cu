@@ -162,11 +162,18 @@ __device__ __forceinline__ unsigned long long pack_stamp(float v, unsigned stamp
 // held in shared memory; the value lands at float i of the window buffer),
 // word i >= tile_words is progress probe i - tile_words (checked, not
 // stored).  Words of cells >= n_cells are never published and read as 0.
-// Polling thread pt of T takes words pt, pt + T, ... in batches of
-// kPollBatch loads in flight.  A batch can be issued early and finished later
-// (the loads overlap other work); every wait is bounded by the launch's
-// timeout (error recorded, false returned).
+// Polling thread pt of T takes words pt, pt + T, ... in batches of NB loads
+// in flight (the step kernel's template parameter: kPollBatchSmall when every
+// polling thread has at most that many words, else kPollBatch).  A batch can
+// be issued early and finished later (the loads overlap other work); every
+// wait is bounded by the launch's timeout (error recorded, false returned).
+// The small batch is the plan's common case and its code is much shorter:
+// on the 10k grid (at most 1,272 words per CTA, 512 threads) 3 slots against
+// 8 took the step from 4.35 to 4.03 us with Kahan sums and from 3.93 to 3.78
+// without; the issue of the loads, not their round trip, was the larger part
+// of the poll.
 constexpr int kPollBatch = 8;
+constexpr int kPollBatchSmall = 3;
 
 struct PollWindow {
   const int* cells;  // the window's sender ids (shared memory)
@@ -183,7 +190,6 @@ struct PollBatchT {
   int dst[NB];  // shared-memory word, or -1 for a probe
   unsigned pend;
 };
-using PollBatch = PollBatchT<kPollBatch>;
 
 // Uncompensated stamped kernels issue the first poll batch of every thread
 // before the gate units and finish it after them (kPollEarly loads per
@@ -193,8 +199,9 @@ using PollBatch = PollBatchT<kPollBatch>;
 // they are needed.  Measured on the 10k grid: 3.93 against 4.10 us per step
 // (the exchange wait falls by a third, the units slow down under the loads
 // in flight); with Kahan sums the step does not gain (4.52 against 4.50 us
-// with per-term compensation, 4.347 against 4.352 with two-term blocks), so
-// Kahan kernels poll after the units.  Two loads
+// with per-term compensation, 4.347 against 4.352 with two-term blocks, 4.08
+// against 4.08 median with the 3-slot poll batch), so Kahan kernels poll after
+// the units.  Two loads
 // per thread leave part of the window to a second round trip (4.56 us); four
 // spill.
 #ifndef INFOLI_POLL_EARLY
@@ -309,22 +316,30 @@ __device__ __forceinline__ bool poll_finish_lean(const StepArgs& a, const unsign
   }
 }
 
+// Takes the words of batch b whose stamp is `want` (their values into tbuf)
+// and clears their pending bits; true when none is left.
 template <int NB>
-__device__ __forceinline__ bool poll_finish(const StepArgs& a, const unsigned long long* src, float* tbuf, int dup,
-                                            unsigned want, PollBatchT<NB>& b, uint64_t& t0) {
-  while (true) {
+__device__ __forceinline__ bool poll_take(float* tbuf, int dup, unsigned want, PollBatchT<NB>& b) {
 #pragma unroll
-    for (int k = 0; k < NB; ++k) {
-      if (((b.pend >> k) & 1u) && (unsigned)(b.w[k] >> 32) == want) {
-        if (b.dst[k] >= 0) {
-          const float v = __uint_as_float((unsigned)b.w[k]) * kVScale;
-          tbuf[b.dst[k]] = v;
-          if (dup) tbuf[dup + b.dst[k]] = v;
-        }
-        b.pend &= ~(1u << k);
+  for (int k = 0; k < NB; ++k) {
+    if (((b.pend >> k) & 1u) && (unsigned)(b.w[k] >> 32) == want) {
+      if (b.dst[k] >= 0) {
+        const float v = __uint_as_float((unsigned)b.w[k]) * kVScale;
+        tbuf[b.dst[k]] = v;
+        if (dup) tbuf[dup + b.dst[k]] = v;
       }
+      b.pend &= ~(1u << k);
     }
-    if (!b.pend) return true;
+  }
+  return b.pend == 0;
+}
+
+// Reloads the pending words of b until all carry `want` (bounded by the
+// launch's timeout: error recorded, false returned).
+template <int NB>
+__device__ __forceinline__ bool poll_retry(const StepArgs& a, const unsigned long long* src, float* tbuf, int dup,
+                                           unsigned want, PollBatchT<NB>& b, uint64_t& t0) {
+  while (true) {
     const uint64_t now = globaltimer_ns();
     if (t0 == 0) {
       t0 = now;
@@ -335,7 +350,29 @@ __device__ __forceinline__ bool poll_finish(const StepArgs& a, const unsigned lo
 #pragma unroll
     for (int k = 0; k < NB; ++k)
       if ((b.pend >> k) & 1u) b.w[k] = ld_poll_u64(src + b.cell[k]);
+    if (poll_take<NB>(tbuf, dup, want, b)) return true;
   }
+}
+
+// The same as a call: the retry loop's code leaves the step loop's hot path.
+template <int NB>
+__device__ __noinline__ bool poll_retry_call(const StepArgs* a, const unsigned long long* src, float* tbuf, int dup,
+                                             unsigned want, PollBatchT<NB> b, uint64_t* t0) {
+  return poll_retry<NB>(*a, src, tbuf, dup, want, b, *t0);
+}
+
+// First look at an issued batch, then the retry loop for words that are not
+// yet current.  OUTLINE runs the retry loop as a call: measured on the 10k
+// grid, the Kahan kernel gains (4.08 -> 3.98 us per step, median) while the
+// uncompensated one loses (3.81 -> 3.95 us) from the call's effect on its
+// register allocation, so only the Kahan kernels use it (with the small
+// batch: the 8-slot batch passed to the call spills).
+template <int NB, bool OUTLINE>
+__device__ __forceinline__ bool poll_finish(const StepArgs& a, const unsigned long long* src, float* tbuf, int dup,
+                                            unsigned want, PollBatchT<NB>& b, uint64_t& t0) {
+  if (poll_take<NB>(tbuf, dup, want, b)) return true;
+  if (OUTLINE) return poll_retry_call<NB>(&a, src, tbuf, dup, want, b, &t0);
+  return poll_retry<NB>(a, src, tbuf, dup, want, b, t0);
 }
 
 // Phase A of stamped plans (packed lane-chunk layout, all in shared memory):
@@ -528,7 +565,7 @@ __device__ __forceinline__ void couple_tile(const ChunkDesc* chunks, const uint1
 
 // BLOCK threads per CTA, one CTA per SM: 1024 threads get 64 registers each,
 // 512 threads 128 (fewer warps, no spills).
-template <int BLOCK, bool KAHAN, bool EDGE_G, bool LL>
+template <int BLOCK, bool KAHAN, bool EDGE_G, bool LL, int NB>
 __global__ void __launch_bounds__(BLOCK, 1) step_kernel(const __grid_constant__ StepArgs a) {
   extern __shared__ __align__(16) unsigned char smem_raw[];
   __shared__ int s_abort;
@@ -585,7 +622,7 @@ __global__ void __launch_bounds__(BLOCK, 1) step_kernel(const __grid_constant__ 
     pw.tile_words = w.n_tiles;  // stamped plans: window words (gcol[tile_begin ..])
     pw.total = pw.tile_words + pw.n_probes;
     const int pollers = (int)blockDim.x - ngroups * U * 32;
-    if (ngroups * U < nwarps && pollers * kPollBatch >= pw.total) poll_first = ngroups * U * 32;
+    if (ngroups * U < nwarps && pollers * NB >= pw.total) poll_first = ngroups * U * 32;
   }
   // (Issuing the first poll batch before the gate units was measured slower:
   // the outstanding loads delay the units' shared-memory traffic.)
@@ -772,10 +809,10 @@ __global__ void __launch_bounds__(BLOCK, 1) step_kernel(const __grid_constant__ 
           ok = poll_finish_lean(a, vsrc, pw, pt, npt, tbuf, shp.dup_words, (unsigned)step, early, pt0);
           base0 = pt + kPollEarly * npt;
         }
-        PollBatch pb;
-        for (int base = base0; ok && base < pw.total; base += kPollBatch * npt) {
+        PollBatchT<NB> pb;
+        for (int base = base0; ok && base < pw.total; base += NB * npt) {
           poll_issue(a, vsrc, pw, base, npt, tbuf, shp.dup_words, pb);
-          ok = poll_finish(a, vsrc, tbuf, shp.dup_words, (unsigned)step, pb, pt0);
+          ok = poll_finish<NB, KAHAN && NB <= kPollBatchSmall>(a, vsrc, tbuf, shp.dup_words, (unsigned)step, pb, pt0);
         }
         if (!ok) s_abort = 1;
       }
@@ -1619,9 +1656,9 @@ cudaError_t launch_gather_block(const StepArgs& a, int grid, cudaStream_t stream
   return g ? launch_gather<BLOCK, false, true>(a, grid, stream) : launch_gather<BLOCK, false, false>(a, grid, stream);
 }
 
-template <int BLOCK, bool K, bool G, bool LL>
+template <int BLOCK, bool K, bool G, bool LL, int NB = kPollBatch>
 cudaError_t launch_variant(const StepArgs& a, int grid, size_t smem, cudaStream_t stream) {
-  auto fn = step_kernel<BLOCK, K, G, LL>;
+  auto fn = step_kernel<BLOCK, K, G, LL, NB>;
   cudaError_t e = cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
   if (e != cudaSuccess) return e;
   void* args[] = {const_cast<StepArgs*>(&a)};
@@ -1632,6 +1669,15 @@ template <int BLOCK>
 cudaError_t launch_block(const StepArgs& a, int grid, size_t smem, cudaStream_t stream) {
   const bool g = a.edge_g != nullptr;
   if (a.shape.stamped) {
+    // the small poll batch when every thread's share of the largest window
+    // fits in it (one round of loads)
+    if (a.shape.poll_words <= kPollBatchSmall * BLOCK) {
+      constexpr int S = kPollBatchSmall;
+      if (a.shape.kahan) return g ? launch_variant<BLOCK, true, true, true, S>(a, grid, smem, stream)
+                                  : launch_variant<BLOCK, true, false, true, S>(a, grid, smem, stream);
+      return g ? launch_variant<BLOCK, false, true, true, S>(a, grid, smem, stream)
+               : launch_variant<BLOCK, false, false, true, S>(a, grid, smem, stream);
+    }
     if (a.shape.kahan) return g ? launch_variant<BLOCK, true, true, true>(a, grid, smem, stream)
                                 : launch_variant<BLOCK, true, false, true>(a, grid, smem, stream);
     return g ? launch_variant<BLOCK, false, true, true>(a, grid, smem, stream)
@@ -1666,11 +1712,11 @@ int max_coresident_ctas(int threads, size_t smem, cudaError_t* err) {
   if (e == cudaSuccess) e = cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev);
   if (e == cudaSuccess) {
     if (threads == 1024) {
-      auto fn = step_kernel<1024, false, false, false>;
+      auto fn = step_kernel<1024, false, false, false, kPollBatch>;
       e = cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
       if (e == cudaSuccess) e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, fn, threads, smem);
     } else if (threads == 512) {
-      auto fn = step_kernel<512, false, false, false>;
+      auto fn = step_kernel<512, false, false, false, kPollBatch>;
       e = cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
       if (e == cudaSuccess) e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, fn, threads, smem);
     } else {

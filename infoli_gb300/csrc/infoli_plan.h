@@ -120,6 +120,8 @@ typedef struct {
                    // tiles cover whole 32-sender columns (TileDesc::chunk_begin /
                    // chunk_end = first / end column); `slices` threads share a row
   int slices;      // bitmask plan: threads per receiver (column slices)
+  int poll_words;  // stamped: the most words one CTA polls per step (window
+                   // senders + progress probes); picks the poll batch size
 } SmemShape;
 
 static inline INFOLI_HD size_t tgather_smem_bytes(SmemShape s) {

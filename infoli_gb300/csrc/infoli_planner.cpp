@@ -943,6 +943,8 @@ bool make_plan_base(const PlanInput& in, Plan* out, std::string* err) {
           if (r != x && reads[r][x] && !reads[x][r]) P.probes.push_back(starts[r]);
         w.n_probes = (int)P.probes.size() - w.probe_begin;
       }
+      sh.poll_words = 0;
+      for (const CtaWork& w : P.cta) sh.poll_words = std::max(sh.poll_words, w.n_tiles + w.n_probes);
     } else if (in.sync_mode == kSyncStamped) {
       *err = "make_plan: stamped exchange requested but the tiles do not fit in shared memory";
       return false;
