@@ -120,7 +120,7 @@ void pack_groups(Plan& P, const SmemLayout& L, const PlanInput& in, const std::v
       std::vector<std::pair<uint16_t, float>> e;
     };
     std::vector<LaneChunk> lc;
-    int slot = 0;
+    int slot = 0, prev_begin = 0;
     for (int r = 0; r < w.n_cells; ++r) {
       const int c = w.cell_begin + r;
       std::vector<std::pair<int, float>> snd;
@@ -128,8 +128,14 @@ void pack_groups(Plan& P, const SmemLayout& L, const PlanInput& in, const std::v
       std::stable_sort(snd.begin(), snd.end(),
                        [](const std::pair<int, float>& x, const std::pair<int, float>& y) { return x.first < y.first; });
       // each receiver's partial slots start on a 4-slot (16-byte) boundary; the
-      // gaps are zeroed once per launch, so the update can read them 4 at a time
+      // gaps are zeroed once per launch, so the update can read them 4 at a time.
+      // Consecutive receivers start an odd number of 16-byte units apart (an
+      // unread unit is added after an even-sized block), so the 8 lanes of each
+      // phase of a 16-byte shared-memory load (one receiver per lane) fall in
+      // 8 different bank groups instead of 2
       slot = (slot + 3) & ~3;
+      if (r > 0 && (((slot - prev_begin) >> 2) & 1) == 0) slot += 4;
+      prev_begin = slot;
       P.cell_slots[c].begin = slot;
       size_t j = 0;  // window position of the sender (senders ascending)
       for (size_t k = 0; k < snd.size(); k += kLaneEdges) {
