@@ -169,14 +169,17 @@ int infoli_read_conn_triples(const char* path, int n, int64_t* row_ptr, int32_t*
  * INFOLI_ERR_CONFIG with the reference's message. */
 int infoli_read_stim_file(const char* path, int n, float* table, int64_t max_rows, int64_t* rows);
 
-/* Randomised initial state (the reference's RAND_INIT, intended behaviour in
+/* Randomised initial state (the reference's RAND_INIT, run by
  * src/single_threaded/infoli.c:206-236, a placeholder in
  * src/openmp/infoli.c:402-422): srand(seed), then g_CaL[c] = 0.6 +
- * 0.2 * (rand() % 100) / 100 for every cell, then every cell c runs
- * k = (rand() % ceil(100 / DELTA)) | 1 steps on its own (no coupling current,
- * no stimulus) from its state in state[19 * n], which is overwritten with the
- * result.  Uses the C library's rand() like the reference (process-wide
- * generator state).  The isolated steps run on the GPU. */
+ * 0.2 * (rand() % 100) / 100 for every cell, then every cell c draws
+ * k = (rand() % ceil(100 / DELTA)) | 1 and runs on its own (no coupling
+ * current, no stimulus) from its state in state[19 * n], which is overwritten
+ * with the state after k - 1 steps: the reference's last isolated step lands
+ * in the state buffer its simulation does not start from
+ * (src/single_threaded/infoli.c:227-228, :293, :316).  Uses the C library's
+ * rand() like the reference (process-wide generator state).  The isolated
+ * steps run on the GPU. */
 int infoli_random_init(const float* params, int n, unsigned seed, float* state, int device);
 
 /* ------------------------------------------------------------------------ */

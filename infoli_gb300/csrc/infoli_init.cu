@@ -1,9 +1,13 @@
 // Randomised initial states: every cell runs a random number of steps on its
-// own (no coupling current, no stimulus) from the configured state, the
-// intent of the reference's RAND_INIT (src/single_threaded/infoli.c:206-236;
-// a placeholder in src/openmp/infoli.c:402-422).  The draws use the C
-// library's rand() in the reference's order; the isolated steps run on the
-// GPU, one thread per cell.
+// own (no coupling current, no stimulus) from the configured state, as the
+// reference's RAND_INIT does (src/single_threaded/infoli.c:206-236; a
+// placeholder in src/openmp/infoli.c:402-422).  The draws use the C library's
+// rand() in the reference's order; the isolated steps run on the GPU, one
+// thread per cell.  The reference draws an odd count k and alternates its two
+// state buffers, step j writing buffer (j % 2) ^ 1 (:227-228), so the last
+// step lands in buffer 1 while the simulation starts from buffer 0 (:293,
+// :316): the state it starts from is the one after k - 1 steps, and that is
+// what is computed here.
 #include <cuda_runtime.h>
 
 #include <cmath>
@@ -93,7 +97,7 @@ extern "C" int infoli_random_init(const float* params, int n, unsigned seed, flo
   for (int c = 0; c < n; ++c) gcal[c] = 0.6 + (0.2 * (rand() % 100) / 100);
   const int span = (int)std::ceil(100 / P.DELTA);
   std::vector<int> steps((size_t)n);
-  for (int c = 0; c < n; ++c) steps[(size_t)c] = (rand() % span) | 1;
+  for (int c = 0; c < n; ++c) steps[(size_t)c] = ((rand() % span) | 1) - 1;  // k drawn, k - 1 kept
   float* d_st = nullptr;
   int* d_steps = nullptr;
   CKI(cudaSetDevice(device));

@@ -15,6 +15,13 @@
 #   oracle/_ref/infoli_omp_perf.x  the OpenMP build again, with the compiler's
 #                                   default floating-point contraction: the CPU
 #                                   baseline that bench.py times
+#   oracle/_ref/single_rand.x      src/single_threaded/infoli.c with its own
+#                                   RAND_INIT switch at 1 (infoli.h:26, "1 for
+#                                   random states"): the source is staged as is in
+#                                   oracle/_ref/rand_init/ beside a copy of its
+#                                   header whose only change is that line (the .c
+#                                   includes "infoli.h" from its own folder); the
+#                                   randomised-state golden generator
 # and the three sources of the OpenMP build plus bin/default.conf are staged,
 # unmodified, in oracle/_ref/src/ (git-ignored, never committed).  A working
 # tree copied to a host without the reference tree (the GPU host, another
@@ -41,6 +48,12 @@ if [ -d "$REF/src/openmp" ]; then
   gcc $CFLAGS -DG_CAL_FROM_FILE "$REF/src/regression_test/stable_version.c" -lm -o "$OUT/stable_version.x"
   gcc -O3 -w "$REF/src/regression_test/regression_checker.c" -lm -o "$OUT/checker.x"
   gcc $PERF_CFLAGS -fopenmp "$REF/src/openmp/infoli.c" "$REF/src/utils/utils.c" -lm -o "$OUT/infoli_omp_perf.x"
+  RND="$OUT/rand_init"
+  mkdir -p "$RND"
+  install -m 644 "$REF/src/single_threaded/infoli.c" "$RND/infoli.c"
+  sed 's/^#define RAND_INIT 0/#define RAND_INIT 1/' "$REF/src/single_threaded/infoli.h" > "$RND/infoli.h"
+  grep -q '^#define RAND_INIT 1' "$RND/infoli.h"
+  gcc $CFLAGS "$RND/infoli.c" -lm -o "$OUT/single_rand.x"
   install -m 644 "$REF/bin/default.conf" "$OUT/default.conf"
   echo "built reference binaries into $OUT"
 elif [ -f "$SRC/infoli.c" ] && [ -f "$SRC/utils.c" ]; then

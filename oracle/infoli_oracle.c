@@ -20,6 +20,9 @@
  *   fused compartment update     src/openmp/infoli.c:556-679
  *   min()                        src/utils/utils.c:340-343
  *   FP64 twin                    src/single_threaded/infoli.c:371-858 (double, exp, pow)
+ *   randomised initial state     src/single_threaded/infoli.c:206-236 (RAND_INIT);
+ *                                pinned on that program built with the switch
+ *                                at 1 (tests/golden/single_rand_init.npz)
  *
  * Build: gcc -O3 -ffp-contract=off -fopenmp -shared -fPIC (see oracle/Makefile).
  * Contraction is off so the float arithmetic matches the reference build and
@@ -452,13 +455,15 @@ int orc_run_f64(int n, const double *params, double *state,
     return rows;
 }
 
-/* Randomised initial state, the intent of RAND_INIT
- * (src/single_threaded/infoli.c:206-236; placeholder in
- * src/openmp/infoli.c:402-422): srand(seed); g_CaL[c] = 0.6 +
- * 0.2 * (rand() % 100) / 100 for every cell, then for every cell
- * k = (rand() % ceil(100 / DELTA)) | 1 steps of the cell alone (no coupling
- * current, no stimulus).  state[19*n] is updated in place; steps_out[n] (may
- * be NULL) receives k. */
+/* Randomised initial state, RAND_INIT (src/single_threaded/infoli.c:206-236;
+ * placeholder in src/openmp/infoli.c:402-422): srand(seed); g_CaL[c] = 0.6 +
+ * 0.2 * (rand() % 100) / 100 for every cell, then for every cell an odd
+ * k = (rand() % ceil(100 / DELTA)) | 1 drawn and the cell run alone (no
+ * coupling current, no stimulus).  The reference alternates two state buffers
+ * (step j reads buffer j % 2 and writes (j % 2) ^ 1, :227-228) and starts the
+ * simulation from buffer 0 (:293, :316), which holds the state after k - 1
+ * steps: that state is the result here.  state[19*n] is updated in place; steps_out[n] (may be
+ * NULL) receives the drawn k. */
 void orc_random_init(int n, const float *params, float *state, unsigned seed, int *steps_out) {
     float *S[ORC_NSTATE];
     for (int i = 0; i < ORC_NSTATE; i++) S[i] = state + (size_t)i * n;
@@ -468,7 +473,7 @@ void orc_random_init(int n, const float *params, float *state, unsigned seed, in
     for (int c = 0; c < n; c++) {
         const int k = (rand() % span) | 1;
         if (steps_out) steps_out[c] = k;
-        for (int j = 0; j < k; j++) cell_f32(params, S, c, 0.0f, 0.0f);
+        for (int j = 0; j < k - 1; j++) cell_f32(params, S, c, 0.0f, 0.0f);
     }
 }
 

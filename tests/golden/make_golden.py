@@ -22,6 +22,13 @@ Fixtures
                               the first 10000 steps (the 'standard' 500 ms
                               check) + every 100th row + spike steps; also the
                               fixture conductance matrix and g_CaL values
+  single_rand_init.npz        src/single_threaded/infoli.c with its RAND_INIT
+                              switch at 1 (oracle/_ref/single_rand.x, seed 1):
+                              randomised initial states (g_CaL and isolated
+                              steps drawn by rand()), then its SIMTIME of 10 ms
+                              (200 steps) in FP64, V_axon every step; on 10
+                              cells coupled by the regression fixture's
+                              conductance matrix and on 64 uncoupled cells
 Usage: python tests/golden/make_golden.py
 """
 from __future__ import annotations
@@ -104,6 +111,21 @@ def main():
     np.savez_compressed(os.path.join(HERE, "kat_stable_version.npz"), v_axon_first10000=v[:10000],
                         v_axon_every100=v[::100], n_steps=v.shape[0], cond_sender_by_receiver=g,
                         gcal=gcal, **{f"spikes_{c}": s for c, s in enumerate(sp)})
+    out = {}
+    for tag, n, cond in (("coupled10", 10, np.loadtxt(os.path.join(src, "cellConnections.txt"))),
+                         ("isolated64", 64, np.zeros((64, 64)))):
+        with tempfile.TemporaryDirectory() as d:
+            with open(os.path.join(d, "cellConnections.txt"), "w") as f:
+                for row in cond:
+                    f.write(" ".join(repr(float(x)) for x in row) + "\n")
+            run(os.path.join(BIN, "single_rand.x"), [str(n)], d)
+            lines = open(os.path.join(d, "InferiorOlive_Output.txt")).read().splitlines()[1:]
+        # rows: " step iApp 1 : v1 2 : v2 ..."; the values are every third token from the fourth
+        v = np.array([[float(t) for t in l.split()[4::3]] for l in lines], dtype=np.float64)
+        assert v.shape == (200, n)
+        out[f"v_axon_{tag}"] = v
+        out[f"cond_sender_by_receiver_{tag}"] = cond.astype(np.float32)
+    np.savez_compressed(os.path.join(HERE, "single_rand_init.npz"), seed=1, **out)
     print("fixtures written to", HERE)
 
 

@@ -128,3 +128,42 @@ def test_removable_singularities_take_their_limits():
     O.run(n, conf[:23].astype(np.float64), s64, rp, col, g_uniform=0.04, nsteps=1, trace_every=0, traces=(),
           fp64=True)
     assert np.isfinite(s64).all()
+
+
+def _dense_to_csr(G):
+    """Conductance matrix, row = sender, column = receiver (the single-threaded
+    reference reads neighId = row index; a zero means no connection)."""
+    n = G.shape[0]
+    rp, col, g = [0], [], []
+    for r in range(n):
+        for s in range(n):
+            if G[s, r] != 0:
+                col.append(s)
+                g.append(G[s, r])
+        rp.append(len(col))
+    return np.array(rp, np.int64), np.array(col, np.int32), np.array(g, np.float32)
+
+
+@pytest.mark.parametrize("tag", ["coupled10", "isolated64"])
+def test_random_init_vs_reference_single_threaded(conf, tag):
+    """Randomised initial states (RAND_INIT) against the reference's own
+    single-threaded build with the switch at 1 (src/single_threaded/
+    infoli.c:206-236, seed 1): the oracle's draws and isolated steps, then 200
+    FP64 steps, follow the reference's V_axon to within the FP32 rounding of the
+    isolated steps.  The reference starts its simulation from the state after
+    k - 1 of the k isolated steps it draws (the last one lands in the buffer the
+    simulation does not read first); with k steps the trajectories differ by
+    about 5e-2 mV, so the tolerance separates the two by two orders of
+    magnitude."""
+    z = golden("single_rand_init.npz")
+    G, ref = z[f"cond_sender_by_receiver_{tag}"], z[f"v_axon_{tag}"]
+    n = G.shape[0]
+    rp, col, g = _dense_to_csr(G)
+    st = O.default_state(n, conf)
+    ks = O.random_init(n, conf, st, int(z["seed"]))
+    assert np.all(ks % 2 == 1) and np.all(ks < 2000)
+    st64 = st.astype(np.float64)
+    got = O.run(n, conf[:23].astype(np.float64), st64, rp, col, g=g, nsteps=200, trace_every=1,
+                traces=("axon",), fp64=True)["axon"]
+    assert got.shape == ref.shape
+    assert np.max(np.abs(got - ref)) < 5e-4
