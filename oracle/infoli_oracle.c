@@ -477,6 +477,22 @@ void orc_random_init(int n, const float *params, float *state, unsigned seed, in
     }
 }
 
+/* The same in double (the single-threaded reference's arithmetic: its state
+ * and g_CaL draw are doubles, its isolated steps CompDend/CompSoma/CompAxon in
+ * double): the FP64 twin's randomised initial state. */
+void orc_random_init_f64(int n, const double *params, double *state, unsigned seed, int *steps_out) {
+    double *S[ORC_NSTATE];
+    for (int i = 0; i < ORC_NSTATE; i++) S[i] = state + (size_t)i * n;
+    srand(seed);
+    for (int c = 0; c < n; c++) S[S_G_CAL][c] = 0.6 + (0.2 * (rand() % 100) / 100);
+    const int span = (int)ceil(100 / params[P_DELTA]);
+    for (int c = 0; c < n; c++) {
+        const int k = (rand() % span) | 1;
+        if (steps_out) steps_out[c] = k;
+        for (int j = 0; j < k - 1; j++) cell_f64(params, S, c, 0.0, 0.0);
+    }
+}
+
 int orc_max_threads(void) {
 #ifdef _OPENMP
     return omp_get_max_threads();

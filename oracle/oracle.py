@@ -59,6 +59,8 @@ def lib():
         L.orc_max_threads.restype = C.c_int
         L.orc_random_init.argtypes = [C.c_int, P, P, C.c_uint, P]
         L.orc_random_init.restype = None
+        L.orc_random_init_f64.argtypes = [C.c_int, P, P, C.c_uint, P]
+        L.orc_random_init_f64.restype = None
         _lib = L
     return _lib
 
@@ -149,12 +151,14 @@ def run(n, params, state, row_ptr, col, g=None, g_uniform=0.04, stim=None,
 
 
 def random_init(n, params, state, seed):
-    """Randomised initial state (orc_random_init); state (19, n) float32 is
-    updated in place; returns the isolated step count of every cell."""
-    assert state.dtype == np.float32 and state.shape == (19, n) and state.flags.c_contiguous
-    params = np.ascontiguousarray(params, dtype=np.float32)
+    """Randomised initial state (orc_random_init, or orc_random_init_f64 for a
+    float64 state); state (19, n) is updated in place; returns the step count
+    drawn for every cell (the state is the one after that count minus one)."""
+    assert state.dtype in (np.float32, np.float64) and state.shape == (19, n) and state.flags.c_contiguous
+    params = np.ascontiguousarray(params, dtype=state.dtype)
     steps = np.zeros(n, dtype=np.int32)
-    lib().orc_random_init(n, _ptr(params), _ptr(state), int(seed) & 0xFFFFFFFF, _ptr(steps))
+    fn = lib().orc_random_init_f64 if state.dtype == np.float64 else lib().orc_random_init
+    fn(n, _ptr(params), _ptr(state), int(seed) & 0xFFFFFFFF, _ptr(steps))
     return steps
 
 

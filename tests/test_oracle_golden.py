@@ -167,3 +167,31 @@ def test_random_init_vs_reference_single_threaded(conf, tag):
                 traces=("axon",), fp64=True)["axon"]
     assert got.shape == ref.shape
     assert np.max(np.abs(got - ref)) < 5e-4
+
+
+def _conf_f64():
+    """default.conf parsed as doubles: the same decimals as the single-threaded
+    reference's constants and initial state (src/single_threaded/infoli.h:33-66,
+    infoli.c:862-889)."""
+    vals = np.array([float(l.split("=")[1]) for l in open(CONF) if "=" in l], dtype=np.float64)
+    assert vals.shape == (42,)
+    return vals
+
+
+@pytest.mark.parametrize("tag", ["coupled10", "isolated64"])
+def test_fp64_twin_vs_reference_single_threaded(built, tag):
+    """The FP64 twin (the FP64 oracle that every accuracy figure of the bench
+    is quoted against) on the single-threaded reference's own FP64 run: its
+    randomised initial state in double, then 200 steps, V_axon every step.  The
+    reference prints 8 decimals (5e-9 mV of rounding); the oracle takes the
+    conductances as float32 (the reference reads them as double)."""
+    z = golden("single_rand_init.npz")
+    G, ref = z[f"cond_sender_by_receiver_{tag}"], z[f"v_axon_{tag}"]
+    n = G.shape[0]
+    rp, col, g = _dense_to_csr(G)
+    vals = _conf_f64()
+    st = np.empty((19, n), dtype=np.float64)
+    st[:] = vals[23:42, None]
+    O.random_init(n, vals[:23], st, int(z["seed"]))
+    got = O.run(n, vals[:23], st, rp, col, g=g, nsteps=200, trace_every=1, traces=("axon",), fp64=True)["axon"]
+    assert np.max(np.abs(got - ref)) < 5e-8
