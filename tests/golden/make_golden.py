@@ -28,7 +28,12 @@ Fixtures
                               steps drawn by rand()), then its SIMTIME of 10 ms
                               (200 steps) in FP64, V_axon every step; on 10
                               cells coupled by the regression fixture's
-                              conductance matrix and on 64 uncoupled cells
+                              conductance matrix and on 64 uncoupled cells;
+                              and on 16 cells (30 % density, conductances
+                              1/32, 3/64, 1/16: exact in binary, so float32 and
+                              double agree) driven by a 400-line stimulus file
+                              (the program's input-file mode, V_axon printed
+                              with 16 decimals)
 Usage: python tests/golden/make_golden.py
 """
 from __future__ import annotations
@@ -125,6 +130,28 @@ def main():
         assert v.shape == (200, n)
         out[f"v_axon_{tag}"] = v
         out[f"cond_sender_by_receiver_{tag}"] = cond.astype(np.float32)
+    rng = np.random.default_rng(7)
+    n = 16
+    cond = np.where(rng.random((n, n)) < 0.3, rng.choice([0.03125, 0.046875, 0.0625], (n, n)), 0.0)
+    np.fill_diagonal(cond, 0.0)
+    amp = rng.choice([0.0, 2.5, 5.0, 7.25], n)
+    onset = rng.integers(0, 300, n)
+    stim = np.array([[amp[c] if onset[c] <= t < onset[c] + 100 else 0.0 for c in range(n)] for t in range(400)])
+    with tempfile.TemporaryDirectory() as d:
+        with open(os.path.join(d, "cellConnections.txt"), "w") as f:
+            for row in cond:
+                f.write(" ".join(repr(float(x)) for x in row) + "\n")
+        with open(os.path.join(d, "stim.txt"), "w") as f:
+            for row in stim:
+                f.write(" ".join("%.4f" % x for x in row) + "\n")
+        run(os.path.join(BIN, "single_rand.x"), [str(n), "stim.txt"], d)
+        lines = open(os.path.join(d, "InferiorOlive_Output.txt")).read().splitlines()[1:]
+    # input-file mode rows: "step time v1 v2 ..."
+    v = np.array([[float(t) for t in l.split()[2:]] for l in lines], dtype=np.float64)
+    assert v.shape == (400, n)
+    out["v_axon_stim16"] = v
+    out["cond_sender_by_receiver_stim16"] = cond.astype(np.float32)
+    out["stim_stim16"] = stim.astype(np.float32)
     np.savez_compressed(os.path.join(HERE, "single_rand_init.npz"), seed=1, **out)
     print("fixtures written to", HERE)
 

@@ -74,3 +74,14 @@ def test_stimulus_file(capi, tmp_path):
     with pytest.raises(capi.InfoliError) as e:
         capi.read_stim_file(str(f), 5)
     assert e.value.code == capi.ERR_CONFIG and "only 3" in str(e.value)
+
+
+def test_stimulus_file_of_the_single_threaded_fixture(capi, tmp_path):
+    """The stimulus file the single-threaded reference ran on (tests/golden/
+    single_rand_init.npz, written with "%.4f " per value as there) reads back
+    as the table the GPU path is given."""
+    tab = golden("single_rand_init.npz")["stim_stim16"]
+    f = tmp_path / "stim.txt"
+    f.write_text("".join(" ".join("%.4f" % x for x in row) + "\n" for row in tab))
+    got = capi.read_stim_file(str(f), tab.shape[1])
+    assert np.array_equal(got, tab)

@@ -195,3 +195,25 @@ def test_fp64_twin_vs_reference_single_threaded(built, tag):
     O.random_init(n, vals[:23], st, int(z["seed"]))
     got = O.run(n, vals[:23], st, rp, col, g=g, nsteps=200, trace_every=1, traces=("axon",), fp64=True)["axon"]
     assert np.max(np.abs(got - ref)) < 5e-8
+
+
+def test_fp64_twin_stimulus_file_vs_reference_single_threaded(built):
+    """The single-threaded reference in its input-file mode (one line of
+    per-cell currents per step, V_axon printed with 16 decimals) on 16 cells
+    whose conductances are exact in binary, after its randomised initial
+    state: the FP64 oracle follows it through the spikes (V_axon up to 48 mV)
+    to 1e-11 mV over 400 steps.  This pins the stimulus table's step alignment
+    (row t drives step t; a shift by one step gives 34 mV), the randomised
+    state and the FP64 cell update together."""
+    z = golden("single_rand_init.npz")
+    G, ref, tab = z["cond_sender_by_receiver_stim16"], z["v_axon_stim16"], z["stim_stim16"]
+    n = G.shape[0]
+    rp, col, g = _dense_to_csr(G)
+    vals = _conf_f64()
+    st = np.empty((19, n), dtype=np.float64)
+    st[:] = vals[23:42, None]
+    O.random_init(n, vals[:23], st, int(z["seed"]))
+    got = O.run(n, vals[:23], st, rp, col, g=g, stim=("table", tab, 0), nsteps=tab.shape[0], trace_every=1,
+                traces=("axon",), fp64=True)["axon"]
+    assert ref.max() > 30.0  # the pulses make cells spike
+    assert np.max(np.abs(got - ref)) < 1e-9
