@@ -50,6 +50,17 @@ def test_reference_generator_networks(capi, n, p, mode):
     assert info["ctas"] >= 1
 
 
+@pytest.mark.parametrize("n,p,ctas", [(500, 0.1, 50), (1000, 0.1, 100), (2000, 0.02, 100), (2000, 0.1, 100),
+                                      (64, 0.5, 7)])
+def test_small_networks_get_the_grid_floor(capi, n, p, ctas):
+    """Small networks get at least min(n / 10, 100) CTAs (the chunk count
+    alone gave 1,000 cells at p = 0.1 25 CTAs: 2.53 against 1.95 us per step
+    with 100), and their plans still give the network's currents."""
+    rp, col = capi.gen_uniform(n, p, 1)
+    info = check(capi, n, rp, col, threads=512)
+    assert info["ctas"] == ctas and info["stamped"] == 1
+
+
 def test_grid_network_10k_stamped(capi):
     rp, col = capi.gen_grid_gaussian(100, 100, 10.0, 18.0, 1)
     info = check(capi, 10000, rp, col, sync_mode=0)
