@@ -103,6 +103,19 @@ def test_grid_gaussian_multi_cta(ig, conf):
     assert np.max(np.abs(gpu["soma"] - ref["soma"])) <= TOL_VSOMA_MV
 
 
+@pytest.mark.parametrize("kahan", [False, True])
+def test_stamped_plan_with_the_wide_poll_batch(ig, conf, kahan):
+    """A stamped plan whose windows are larger than 3 words per thread (10,000
+    cells with 100 uniform random senders each: about 4,850 unique senders per
+    CTA of 512 threads), so the step kernel polls with its 8-slot batch rather
+    than the 3-slot one of the 10k grid."""
+    n = 10000
+    rp, col = ig.gen_uniform(n, 0.01, 2)
+    st0 = hetero_state(conf, n, 9)
+    gpu, ref, _, _ = _compare(ig, conf, n, rp, col, st0, steps=300, kahan=kahan, nthreads=16)
+    assert np.max(np.abs(gpu["soma"] - ref["soma"])) <= TOL_VSOMA_MV
+
+
 @pytest.mark.parametrize("kahan,mode", [(False, "auto"), (True, "auto"), (True, "gather"), (True, "tgather")])
 def test_per_edge_g_and_cell_pulses_spike_times(ig, conf, kahan, mode, monkeypatch):
     """CSR with per-edge g ~ U(0.02,0.06), per-cell 5 ms pulses: V_soma over the
