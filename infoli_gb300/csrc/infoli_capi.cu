@@ -237,6 +237,36 @@ int upload_state(infoli_sim* s, const float* state /*19 x n*/) {
   return INFOLI_OK;
 }
 
+// The same at creation, by copies only: the state is repacked on the host
+// (19 x n floats -> the device's field rows, FP64 Ca2+, V_dend in both halves
+// of its double buffer) and moved with one copy per array on the copy
+// engines.  A kernel here would wait for free SMs while other simulations'
+// persistent grids hold them all, which made a serving request's preparation
+// wait for the running requests.  Padding cells stay as they are, as with
+// the scatter.
+int upload_state_copies(infoli_sim* s, const float* state /*19 x n*/) {
+  const int n = s->n;
+  const size_t np = (size_t)s->n_pad;
+  std::vector<double> ca((size_t)n);
+  for (int k = 0; k < INFOLI_NSTATE; ++k) {
+    const float* src = state + (size_t)k * n;
+    const int f = kFieldOfState[k];
+    if (f == -1) {
+      CK(cudaMemcpyAsync(s->d_vd[s->step & 1], src, (size_t)n * sizeof(float), cudaMemcpyHostToDevice, s->stream));
+      CK(cudaMemcpyAsync(s->d_vd[(s->step + 1) & 1], src, (size_t)n * sizeof(float), cudaMemcpyHostToDevice,
+                         s->stream));
+    } else if (f == -2) {
+      for (int c = 0; c < n; ++c) ca[(size_t)c] = (double)src[c];
+      CK(cudaMemcpyAsync(s->d_ca, ca.data(), (size_t)n * sizeof(double), cudaMemcpyHostToDevice, s->stream));
+    } else {
+      CK(cudaMemcpyAsync(s->d_st + (size_t)f * np, src, (size_t)n * sizeof(float), cudaMemcpyHostToDevice,
+                         s->stream));
+    }
+  }
+  CK(cudaStreamSynchronize(s->stream));
+  return INFOLI_OK;
+}
+
 int fill_args(infoli_sim* s, StepArgs* a) {
   std::memset(a, 0, sizeof *a);
   a->P = s->P;
@@ -462,7 +492,7 @@ int infoli_sim_create(const infoli_sim_desc* d, infoli_sim** out) {
       std::fill(init.begin() + (size_t)k * s->n, init.begin() + (size_t)(k + 1) * s->n, d->init_values[k]);
     st = init.data();
   }
-  if ((rc = upload_state(s, st))) return fail(rc);
+  if ((rc = upload_state_copies(s, st))) return fail(rc);
   for (int i = 0; i < 2; ++i)
     if (cudaEventCreateWithFlags(&s->ev_kernel[i], cudaEventDisableTiming) != cudaSuccess ||
         cudaEventCreateWithFlags(&s->ev_copy[i], cudaEventDisableTiming) != cudaSuccess)
