@@ -132,7 +132,7 @@ def test_c2_grid10k_spike_steps_two_seconds(ig, conf, request):
 
     cfg, n, rp, col, st0 = bench.workload()
     err, gsp, rsp = run_both(ig, cfg, n, rp, col, st0, 40000, 2000)
-    # the spec window: 1 s simulated from the pulse onset (steps 20,000-39,999)
+    # the window of the stated criterion: 1 s simulated from the pulse onset (steps 20,000-39,999)
     first_s = [[s for s in x if s < 20000] for x in rsp]
     total, bad = _report(request, "C2 10k grid, 40,000 steps", err, gsp, rsp,
                          extra=f"; oracle spikes before step 20,000: {sum(len(x) for x in first_s)}")
