@@ -15,6 +15,11 @@ Fixtures
   omp_n200_p0.1_t30.txt       reference OpenMP build (normal trace format,
                               tagged, every 100th step), seed 1,
                               -n 200 -p 0.1 -t 30, header line 1 blanked
+  omp_test_n1000_p0.1_t5.npz  reference OpenMP build, -DG_CAL_FROM_FILE, seed
+                              1, -n 1000 -p 0.1 -t 5 (the C1 configuration's
+                              network with per-cell g_CaL, so the cells differ
+                              and the coupling acts; 100 steps): V_axon of every
+                              10th step plus the g_CaL values it read
   kat_stable_version.npz      the reference's regression golden generator
                               (src/regression_test/stable_version.c) on its
                               own fixtures (10 cells, cellConnections.txt,
@@ -102,6 +107,11 @@ def main():
     lines[0] = "Execution Time for Simulation in ms: <timing>"
     with open(os.path.join(HERE, "omp_n200_p0.1_t30.txt"), "w") as f:
         f.write("\n".join(lines))
+
+    v, gcal, txt = omp_test_case(1000, 0.1, 5, 11)
+    assert v.shape == (100, 1000)
+    np.savez_compressed(os.path.join(HERE, "omp_test_n1000_p0.1_t5.npz"), v_axon_every10=v[9::10], gcal=gcal,
+                        gcal_text=np.array(txt), n=1000, p=np.float32(0.1), t=np.float32(5), seed=1)
 
     src = os.path.join(REF, "src", "regression_test")
     with tempfile.TemporaryDirectory() as d:

@@ -44,6 +44,23 @@ def test_oracle_bit_exact_vs_reference_omp_test(conf):
     assert np.array_equal(_fmt8(tr), z["v_axon"])
 
 
+def test_oracle_bit_exact_vs_reference_at_the_c1_size(conf):
+    """The C1 configuration's network (1,000 cells, the reference generator at
+    p = 0.1, seed 1) with per-cell g_CaL (the plain run's identical cells
+    would leave the coupling at zero), 100 steps against the reference's
+    omp_test build: every 10th row byte-identical."""
+    z = golden("omp_test_n1000_p0.1_t5.npz")
+    n = int(z["n"])
+    rp, col = O.gen_uniform(n, np.float32(z["p"]), int(z["seed"]))
+    st = O.default_state(n, conf)
+    st[O.S["g_CaL"]] = z["gcal"]
+    steps = int(np.float32(z["t"]) / conf[0])
+    tr = O.run(n, conf[:23], st, rp, col, g_uniform=conf[1], nsteps=steps, trace_every=1,
+               traces=("axon",), nthreads=O.max_threads())["axon"]
+    assert np.array_equal(_fmt8(tr[9::10]), z["v_axon_every10"])
+    assert np.std(z["v_axon_every10"][-1]) > 1e-4  # the cells differ
+
+
 def test_oracle_bit_exact_through_spikes(conf):
     """20 cells, 22000 steps with the 6 uA pulse: same rows and spike steps."""
     z = golden("omp_test_n20_p0.5_t1100.npz")
